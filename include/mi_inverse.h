@@ -1,0 +1,92 @@
+/*
+ * mi_inverse.h -- C ABI of the GB300 batched small-matrix inverter.
+ *
+ * Plain pointers and sizes only.  All device pointers are caller-owned CUDA
+ * device memory; every call is stream-ordered on `stream` (a cudaStream_t, or
+ * NULL for the legacy default stream), returns a status code and never exits
+ * the process.
+ *
+ * What each entry point replaces in the reference (sumukhashridhar/
+ * matrixInversion; paths relative to its root):
+ *   mi_inverse_f32      batched_lu_subwarp<float, n, T, mpb, N><<<ceil(N/mpb),
+ *                       NUMTHREADS, smem>>>(d_A) -- parallel_pivot/
+ *                       luBatchedInplace.cu:127 (pivot = MI_PIVOT_REFERENCE),
+ *                       serial_pivot/luBatchedInplace.cu:105
+ *                       (MI_PIVOT_REFERENCE_SERIAL), templated/
+ *                       luBatchedInplace.cu:76 (MI_PIVOT_NONE).  In place,
+ *                       row-major, matrix b at offset b*n*n, as there.  The
+ *                       reference keeps its pivots in shared memory
+ *                       (parallel_pivot/luBatchedInplace.cuh:140); here they
+ *                       can be written out (d_perm).
+ *   mi_inverse_cfg_f32  the same launch with the reference's NUMTHREADS knob
+ *                       (threads per block; parallel_pivot/run.py:41, 187-224)
+ *                       and an explicit grid size.
+ *   mi_query_config     the launch geometry the reference derives in
+ *                       luBatchedInplace.cu:8-11 (threads per matrix,
+ *                       matrices per block) and :118 (shared memory).
+ *   mi_error_string /   the reference's CUDA_CHECK, which prints and calls
+ *   mi_last_cuda_error  exit(1) (parallel_pivot/luBatchedInplace.cuh:9).
+ */
+#ifndef MI_INVERSE_H
+#define MI_INVERSE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MI_ABI_VERSION 1
+
+/* status codes */
+#define MI_OK 0
+#define MI_ERR_INVALID_VALUE (-1) /* n outside 1..32, batch < 0, unknown pivot mode, bad knob */
+#define MI_ERR_NULL_POINTER (-2)  /* d_a is NULL while batch > 0 */
+#define MI_ERR_MISALIGNED (-3)    /* d_a not 4-byte aligned */
+#define MI_ERR_CUDA (-4)          /* a CUDA call failed; see mi_last_cuda_error() */
+
+/* pivot modes */
+#define MI_PIVOT_NONE 0             /* plain LU (templated/ kernel)                  */
+#define MI_PIVOT_REFERENCE 1        /* parallel_pivot/ argmax tree, bit-exact pivots */
+#define MI_PIVOT_REFERENCE_SERIAL 2 /* serial_pivot/ sequential argmax               */
+#define MI_PIVOT_PARTIAL 3          /* textbook partial pivoting (getrf semantics)   */
+
+/*
+ * Invert `batch` row-major n x n FP32 matrices in place: d_a[b*n*n ...] is
+ * replaced by its inverse.
+ *   d_perm  (nullable) int32[batch][n]: d_perm[b][i] = input row that ends at
+ *           row i after the pivoting (the reference's shared pivots[]); the
+ *           inverse satisfies A^-1[:, perm[i]] = (P A)^-1[:, i].
+ *   d_info  (nullable) int32[batch]: 0, or k (1-based) if the k-th pivot was
+ *           exactly zero (the inverse then holds inf/NaN, as the reference's).
+ */
+int mi_inverse_f32(float* d_a, int32_t* d_perm, int32_t* d_info, int64_t batch, int n, int pivot,
+                   void* stream);
+
+/*
+ * As mi_inverse_f32 with explicit launch knobs.
+ *   threads_per_block  the NUMTHREADS knob; rounded up to a multiple of 32 and
+ *                      capped at 256; 0 = default.
+ *   grid_blocks        0 = sized from the device's SM count and occupancy.
+ */
+int mi_inverse_cfg_f32(float* d_a, int32_t* d_perm, int32_t* d_info, int64_t batch, int n, int pivot,
+                       int threads_per_block, int grid_blocks, void* stream);
+
+/*
+ * Launch geometry for size n: lanes per matrix, matrices per warp, shared
+ * memory bytes per warp, and the default threads per block.  Any out pointer
+ * may be NULL.  Needs no GPU.
+ */
+int mi_query_config(int n, int* lanes_per_matrix, int* matrices_per_warp, int* smem_bytes_per_warp,
+                    int* default_threads_per_block);
+
+const char* mi_error_string(int status);
+/* Text of the last CUDA error seen by this thread ("" if none). */
+const char* mi_last_cuda_error(void);
+int mi_abi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MI_INVERSE_H */

@@ -1,0 +1,80 @@
+"""ctypes binding of ``lib/libmi_inverse.so`` (the C ABI in include/mi_inverse.h).
+
+Loading fails loudly when the library has not been built: there is no
+CPU or framework fallback behind this module.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+from . import build as _build
+
+MI_OK = 0
+MI_ERR_INVALID_VALUE = -1
+MI_ERR_NULL_POINTER = -2
+MI_ERR_MISALIGNED = -3
+MI_ERR_CUDA = -4
+
+PIVOT_MODES = {"none": 0, "reference": 1, "reference_serial": 2, "partial": 3}
+
+_lib = None
+
+
+class MatrixInversionError(RuntimeError):
+    """A non-zero status from the C ABI."""
+
+    def __init__(self, status: int, message: str):
+        super().__init__(f"mi status {status}: {message}")
+        self.status = status
+
+
+def load(path: str | None = None):
+    """Load (once) and type the shared library."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or _build.LIB
+    if not os.path.exists(path):
+        raise RuntimeError(
+            f"CUDA library {path} is not built; run matrixinversion_gb300.build.build() "
+            "(or __graft_entry__.build()) first"
+        )
+    L = ctypes.CDLL(path)
+    vp, i32, i64 = ctypes.c_void_p, ctypes.c_int, ctypes.c_int64
+    L.mi_inverse_f32.argtypes = [vp, vp, vp, i64, i32, i32, vp]
+    L.mi_inverse_f32.restype = i32
+    L.mi_inverse_cfg_f32.argtypes = [vp, vp, vp, i64, i32, i32, i32, i32, vp]
+    L.mi_inverse_cfg_f32.restype = i32
+    ip = ctypes.POINTER(ctypes.c_int)
+    L.mi_query_config.argtypes = [i32, ip, ip, ip, ip]
+    L.mi_query_config.restype = i32
+    L.mi_error_string.argtypes = [i32]
+    L.mi_error_string.restype = ctypes.c_char_p
+    L.mi_last_cuda_error.argtypes = []
+    L.mi_last_cuda_error.restype = ctypes.c_char_p
+    L.mi_abi_version.argtypes = []
+    L.mi_abi_version.restype = i32
+    _lib = L
+    return L
+
+
+def check(status: int) -> None:
+    if status != MI_OK:
+        L = load()
+        msg = L.mi_error_string(status).decode()
+        if status == MI_ERR_CUDA:
+            msg += ": " + L.mi_last_cuda_error().decode()
+        raise MatrixInversionError(status, msg)
+
+
+def exported_symbols() -> list[str]:
+    """Entry points declared in include/mi_inverse.h (the C ABI surface)."""
+    return [
+        "mi_inverse_f32",
+        "mi_inverse_cfg_f32",
+        "mi_query_config",
+        "mi_error_string",
+        "mi_last_cuda_error",
+        "mi_abi_version",
+    ]

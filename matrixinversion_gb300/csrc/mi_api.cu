@@ -1,0 +1,108 @@
+// mi_api.cu -- the C ABI declared in include/mi_inverse.h.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+
+#include "mi_inverse.h"
+#include "mi_launch.cuh"
+
+namespace mi {
+
+static thread_local char g_last_cuda_error[256] = "";
+
+static int cuda_fail(cudaError_t e, const char* what) {
+    std::snprintf(g_last_cuda_error, sizeof(g_last_cuda_error), "%s: %s (%d)", what, cudaGetErrorString(e), (int)e);
+    return MI_ERR_CUDA;
+}
+
+int device_sm_count() {
+    static int cached[64] = {0};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 1;
+    if (dev >= 0 && dev < 64 && cached[dev] > 0) return cached[dev];
+    int sms = 1;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1) sms = 1;
+    if (dev >= 0 && dev < 64) cached[dev] = sms;
+    return sms;
+}
+
+template <int N>
+static void geom_of(int& lanes, int& mpw, int& smem_warp) {
+    lanes = Geom<N>::L;
+    mpw = Geom<N>::M;
+    smem_warp = Geom<N>::kPerWarp * (int)sizeof(float);
+}
+
+static bool query(int n, int& lanes, int& mpw, int& smem_warp) {
+    switch (n) {
+#define MI_Q(K) case K: geom_of<K>(lanes, mpw, smem_warp); return true;
+        MI_Q(1) MI_Q(2) MI_Q(3) MI_Q(4) MI_Q(5) MI_Q(6) MI_Q(7) MI_Q(8)
+        MI_Q(9) MI_Q(10) MI_Q(11) MI_Q(12) MI_Q(13) MI_Q(14) MI_Q(15) MI_Q(16)
+        MI_Q(17) MI_Q(18) MI_Q(19) MI_Q(20) MI_Q(21) MI_Q(22) MI_Q(23) MI_Q(24)
+        MI_Q(25) MI_Q(26) MI_Q(27) MI_Q(28) MI_Q(29) MI_Q(30) MI_Q(31) MI_Q(32)
+#undef MI_Q
+        default: return false;
+    }
+}
+
+}  // namespace mi
+
+extern "C" {
+
+int mi_abi_version(void) { return MI_ABI_VERSION; }
+
+const char* mi_error_string(int status) {
+    switch (status) {
+        case MI_OK: return "ok";
+        case MI_ERR_INVALID_VALUE: return "invalid value (n outside 1..32, batch < 0, unknown pivot mode or bad knob)";
+        case MI_ERR_NULL_POINTER: return "null matrix pointer with batch > 0";
+        case MI_ERR_MISALIGNED: return "matrix pointer is not 4-byte aligned";
+        case MI_ERR_CUDA: return "CUDA error (see mi_last_cuda_error)";
+        default: return "unknown status";
+    }
+}
+
+const char* mi_last_cuda_error(void) { return mi::g_last_cuda_error; }
+
+int mi_query_config(int n, int* lanes_per_matrix, int* matrices_per_warp, int* smem_bytes_per_warp,
+                    int* default_threads_per_block) {
+    int lanes = 0, mpw = 0, smem = 0;
+    if (!mi::query(n, lanes, mpw, smem)) return MI_ERR_INVALID_VALUE;
+    if (lanes_per_matrix) *lanes_per_matrix = lanes;
+    if (matrices_per_warp) *matrices_per_warp = mpw;
+    if (smem_bytes_per_warp) *smem_bytes_per_warp = smem;
+    if (default_threads_per_block) *default_threads_per_block = mi::kDefaultThreadsPerBlock;
+    return MI_OK;
+}
+
+int mi_inverse_cfg_f32(float* d_a, int32_t* d_perm, int32_t* d_info, int64_t batch, int n, int pivot,
+                       int threads_per_block, int grid_blocks, void* stream) {
+    if (n < 1 || n > 32 || batch < 0 || threads_per_block < 0 || grid_blocks < 0) return MI_ERR_INVALID_VALUE;
+    const mi::launch_fn* table = nullptr;
+    switch (pivot) {
+        case MI_PIVOT_NONE: table = mi::kTableNone; break;
+        case MI_PIVOT_REFERENCE: table = mi::kTableReference; break;
+        case MI_PIVOT_REFERENCE_SERIAL: table = mi::kTableReferenceSerial; break;
+        case MI_PIVOT_PARTIAL: table = mi::kTablePartial; break;
+        default: return MI_ERR_INVALID_VALUE;
+    }
+    if (batch == 0) return MI_OK;
+    if (d_a == nullptr) return MI_ERR_NULL_POINTER;
+    if ((reinterpret_cast<uintptr_t>(d_a) & 3u) != 0) return MI_ERR_MISALIGNED;
+    int tpb = threads_per_block == 0 ? mi::kDefaultThreadsPerBlock : threads_per_block;
+    tpb = (tpb + 31) / 32 * 32;
+    if (tpb > mi::kMaxThreadsPerBlock) tpb = mi::kMaxThreadsPerBlock;
+    cudaError_t e = table[n](d_a, d_perm, d_info, (long long)batch, tpb, grid_blocks,
+                             reinterpret_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return mi::cuda_fail(e, "mi_inverse launch");
+    return MI_OK;
+}
+
+int mi_inverse_f32(float* d_a, int32_t* d_perm, int32_t* d_info, int64_t batch, int n, int pivot,
+                   void* stream) {
+    return mi_inverse_cfg_f32(d_a, d_perm, d_info, batch, n, pivot, 0, 0, stream);
+}
+
+}  // extern "C"

@@ -1,0 +1,6 @@
+// Instantiations of the inverse kernel for n = 1..32, pivot mode reference_serial.
+#include "mi_launch.cuh"
+
+namespace mi {
+MI_TABLE(kTableReferenceSerial, kModeReferenceSerial);
+}  // namespace mi

@@ -1,0 +1,117 @@
+"""The oracle against the reference's own kernels (golden pivots) and known answers.
+
+CPU only.  The golden file was produced by running the reference's kernel
+headers unchanged on host threads (tests/golden/make_golden.py).
+"""
+import zlib
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+
+def test_mt19937_stream_matches_numpy(oracle):
+    # MT19937(seed 0) first outputs, and the float mapping, against numpy's
+    # independent implementation of the same generator
+    a = oracle.uniform(0, 4, 8).reshape(-1)
+    b = oracle.uniform_numpy(0, a.size)
+    assert np.array_equal(a, b)
+    assert a.min() >= -1.0 and a.max() < 1.0
+    u = np.random.RandomState(0).randint(0, 2**32, size=1, dtype=np.uint32)[0]
+    assert u == 2357136044  # std::mt19937(0)()
+
+
+@pytest.mark.parametrize("n", range(1, 33))
+def test_pivots_match_reference_kernels_uniform(oracle, golden, n):
+    seed, count = golden[f"n{n}_uniform_seed"]
+    A = oracle.uniform(int(seed), int(count), n)
+    assert zlib.crc32(A.tobytes()) == int(golden[f"n{n}_uniform_crc"][0])
+    assert np.array_equal(oracle.pivots(A, "reference"), golden[f"n{n}_uniform_piv_parallel"])
+    assert np.array_equal(oracle.pivots(A, "reference_serial"), golden[f"n{n}_uniform_piv_serial"])
+
+
+@pytest.mark.parametrize("n", range(1, 33))
+def test_pivots_match_reference_kernels_ties_and_nan(oracle, golden, n):
+    T = golden[f"n{n}_ties_A"].astype(np.float32)
+    assert np.array_equal(oracle.pivots(T, "reference"), golden[f"n{n}_ties_piv_parallel"])
+    assert np.array_equal(oracle.pivots(T, "reference_serial"), golden[f"n{n}_ties_piv_serial"])
+    Z = golden[f"n{n}_nan_A"]
+    assert np.array_equal(oracle.pivots(Z, "reference"), golden[f"n{n}_nan_piv_parallel"])
+    assert np.array_equal(oracle.pivots(Z, "reference_serial"), golden[f"n{n}_nan_piv_serial"])
+
+
+def test_reference_fixtures(oracle, golden):
+    lit = golden["literal4_A"]
+    assert np.array_equal(oracle.pivots(lit, "reference"), golden["literal4_piv_parallel"])
+    assert np.array_equal(oracle.pivots(lit, "reference_serial"), golden["literal4_piv_serial"])
+    tmpl = golden["mtrand32_template"]
+    for n in range(1, 33):
+        M = tmpl[: n * n].reshape(1, n, n).copy()
+        assert np.array_equal(oracle.pivots(M, "reference"), golden[f"mtrand_n{n}_piv_parallel"]), n
+        assert np.array_equal(oracle.pivots(M, "reference_serial"), golden[f"mtrand_n{n}_piv_serial"]), n
+
+
+def test_parallel_rule_drops_tree_slots(oracle):
+    # n = 6: the stride-3,1 tree never merges slot 2 (row k+3) into slot 0, so a
+    # unique maximum there is ignored, while the serial scan takes it.
+    A = np.eye(6, dtype=np.float32)[None] * 0.1
+    A[0, 3, 0] = 5.0
+    assert oracle.pivots(A, "reference")[0, 0] == 0
+    assert oracle.pivots(A, "reference_serial")[0, 0] == 3
+
+
+@pytest.mark.parametrize("n", range(1, 33))
+def test_templated_inverse_matches_oracle(oracle, golden, n):
+    D, Xt = golden[f"n{n}_nopiv_A"], golden[f"n{n}_nopiv_X"]
+    X64, _, info = oracle.inverse_f64(D, "none")
+    assert (info == 0).all()
+    assert np.abs(Xt - X64).max() <= 1e-5 * max(1.0, np.abs(X64).max())
+
+
+@pytest.mark.parametrize("mode", ["reference", "reference_serial", "partial", "none"])
+def test_f64_inverse_is_an_inverse(oracle, mode):
+    n = 12
+    A = oracle.uniform(5, 64, n) + (np.float32(n) * np.eye(n, dtype=np.float32) if mode == "none" else 0)
+    X, perm, info = oracle.inverse_f64(A, mode)
+    assert (info == 0).all()
+    for b in range(A.shape[0]):
+        assert sorted(perm[b]) == list(range(n))
+        assert np.abs(A[b].astype(np.float64) @ X[b] - np.eye(n)).max() < 1e-9
+
+
+def test_partial_pivots_match_lapack(oracle):
+    scipy_linalg = pytest.importorskip("scipy.linalg")
+    n = 16
+    A = oracle.uniform(11, 50, n)
+    _, perm, _ = oracle.inverse_f64(A, "partial")
+    for b in range(A.shape[0]):
+        _, piv = scipy_linalg.lu_factor(A[b].astype(np.float64))
+        p = list(range(n))
+        for k, q in enumerate(piv):
+            p[k], p[q] = p[q], p[k]
+        assert list(perm[b]) == p
+
+
+def test_port_residuals_and_singular_info(oracle):
+    n = 8
+    A = oracle.uniform(3, 32, n)
+    X, perm, info = oracle.ref_inverse_f32(A, "reference")
+    assert np.array_equal(perm, oracle.pivots(A, "reference"))
+    res = oracle.residual(A, X)
+    assert np.median(res[:, 0]) < 1e-3
+    S = np.zeros((1, n, n), dtype=np.float32)
+    _, _, info = oracle.inverse_f64(S, "partial")
+    assert info[0] == 1
+
+
+def test_live_reference_emulation_agrees(oracle):
+    """Fresh seeds against the reference kernels (only where their sources are)."""
+    if not oracle.ref_available():
+        pytest.skip("reference emulation not built here")
+    for n in (5, 11, 24, 32):
+        A = oracle.uniform(777 + n, 6, n)
+        _, pp = oracle.ref_kernel_run("parallel_pivot", A)
+        _, ps = oracle.ref_kernel_run("serial_pivot", A)
+        assert np.array_equal(pp, oracle.pivots(A, "reference"))
+        assert np.array_equal(ps, oracle.pivots(A, "reference_serial"))
