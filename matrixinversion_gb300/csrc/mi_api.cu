@@ -4,6 +4,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 
 #include "mi_inverse.h"
 #include "mi_launch.cuh"
@@ -28,11 +29,27 @@ int device_sm_count() {
     return sms;
 }
 
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    });
+    return fn;
+}
+
 template <int N>
 static void geom_of(int& lanes, int& mpw, int& smem_warp) {
-    lanes = Geom<N>::L;
-    mpw = Geom<N>::M;
-    smem_warp = Geom<N>::kPerWarp * (int)sizeof(float);
+    constexpr int L = default_lanes(N, kModeReference);
+    lanes = L;
+    mpw = Geom<N, L>::M;
+    // two staged tiles plus the per-matrix scratch, per warp
+    smem_warp = (int)(smem_bytes<N, L>(1) - 1024 - 16);
 }
 
 static bool query(int n, int& lanes, int& mpw, int& smem_warp) {

@@ -2,79 +2,120 @@
 // for sm_103a.
 //
 // Method (the reference's: LU with optional row pivoting, then the inverse
-// from the triangular factors and the row permutation), scheduled for a GPU
-// warp instead of the reference's shared-memory Doolittle sweep
+// from the triangular factors and the row permutation), scheduled for warps
+// instead of the reference's one-thread-per-column shared-memory sweep
 // (parallel_pivot/luBatchedInplace.cuh:127-199):
 //
-//   * One sub-warp of L lanes (4/8/16/32, by n) owns a matrix; a warp holds
-//     32/L matrices.  Lane (rg, cg) keeps an R x C register block of the
-//     matrix (rows rg*R.., columns cg*C..), so every step is register FMAs.
+//   * Data movement: a CTA of W warps works on tiles of W*M matrices.  Tiles
+//     stream HBM -> shared memory through the TMA engine (a 3-D tensor copy
+//     with the 128-byte swizzle for n = 32, a 1-D bulk copy otherwise), two
+//     tiles in flight per CTA (the next tile loads while this one computes),
+//     and results leave the same way, so the SMs issue no per-element loads
+//     or stores.  Ragged tails and unaligned pointers use plain loads.
+//   * One sub-warp of L lanes owns a matrix (a warp holds M = 32/L).  Lane
+//     (rg, cg) keeps an R x C register block: rows rg, rg+RG, ... (cyclic),
+//     columns cg*C .. cg*C+C-1.
 //   * Step k applies the k-th LU elimination to the rows below the pivot and
-//     the k-th triangular-inverse update to the rows above it, in the
-//     product (Gauss-Jordan) form: a[i][j] -= (a[i][k]/a[k][k]) * a[k][j].
-//     Below the pivot this is exactly the Schur-complement update of
-//     right-looking LU, so pivot values, info and the partial-pivot argmax see
-//     the same numbers as getrf; after n steps the block holds (PA)^-1 and
-//     A^-1 = (PA)^-1 P is stored by permuting columns.  Each step is one full
-//     rank-1 update (n^2 FMAs), n^3 FMAs in total = the 2n^3 flops of
-//     getrf + getri, with no idle lanes on triangular shapes.
-//   * The pivot row is kept unscaled (its diagonal set to 1) and every row is
-//     scaled by its 1/pivot once at the end, so a step is: broadcast column k
-//     and row k through shared memory, one reciprocal, 2 packed multiplies and
-//     R*C/2 packed FMAs (fma.rn.f32x2).
+//     the k-th triangular-inverse update to the rows above it, in product
+//     (Gauss-Jordan) form, a[i][j] -= (a[i][k] / a[k][k]) a[k][j].  Below the
+//     pivot this is exactly right-looking LU's Schur-complement update, so the
+//     pivot values, info and the partial-pivoting argmax see the numbers getrf
+//     sees; after n steps the block holds (PA)^-1, and A^-1 = (PA)^-1 P is
+//     stored by permuting columns.  Every step is one full rank-1 update
+//     (n^2 FMAs): n^3 FMAs in all, the 2n^3 flops of getrf + getri, with no
+//     lanes idling on triangular shapes.
+//   * The pivot row is kept unscaled (its diagonal entry set to 1) and every
+//     row is scaled by its 1/pivot once at the end, so a step is: column k and
+//     row k broadcast through shared memory, one reciprocal, R/2 packed
+//     multiplies and R*C/2 packed FMAs (fma.rn.f32x2).
 //   * Pivoting:
-//       reference         -- the reference's parallel-argmax rule
-//                            (find_pivot_parallel, parallel_pivot/
-//                            luBatchedInplace.cuh:12-44, T = n slots): it reads
-//                            only raw input entries, so the whole pivot
-//                            sequence is replayed first, lane = row, with
-//                            warp max-reductions (ties broken in the tree's
-//                            own order), and the rows are then loaded in
-//                            pivot order.
-//       reference_serial  -- serial_pivot's sequential argmax
-//                            (serial_pivot/luBatchedInplace.cuh:22-36).
-//       partial           -- textbook partial pivoting on the updated column
-//                            (getrf: first maximum, rows exchanged in place).
-//       none              -- templated/luBatchedInplace.cuh:78-126's plain LU.
+//       reference        -- the reference's parallel argmax (find_pivot_parallel,
+//                           parallel_pivot/luBatchedInplace.cuh:12-44, with
+//                           T = n slots).  It compares raw input entries only
+//                           (columns k, rows >= k are never written before step
+//                           k), so the whole pivot sequence is replayed before
+//                           the elimination, lane = row, with warp max
+//                           reductions; when the maximum is unique no position
+//                           bookkeeping is needed, and ties or NaNs fall back to
+//                           an exact replay of the tree (slot order, dropped
+//                           slots of non-power-of-two n).  Rows are then loaded
+//                           in pivot order.
+//       reference_serial -- serial_pivot's sequential argmax
+//                           (serial_pivot/luBatchedInplace.cuh:22-36).
+//       partial          -- textbook partial pivoting on the updated column
+//                           (getrf: first maximum, rows exchanged in place).
+//       none             -- templated/luBatchedInplace.cuh:78-126's plain LU.
 //   * Outputs: A^-1 in place, optional perm[b][i] (input row that ends at row
-//     i, the reference's shared pivots[] array) and info[b] (0, or the 1-based
-//     step of the first exactly-zero pivot, as getrf's info).
+//     i, the reference's shared pivots[]) and info[b] (0, or the 1-based step
+//     of the first exactly-zero pivot, as getrf's info).
 #pragma once
 
-#include <cstdint>
+#include <cuda.h>
 #include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "mi_ptx.cuh"
 
 namespace mi {
 
 enum : int { kModeNone = 0, kModeReference = 1, kModeReferenceSerial = 2, kModePartial = 3 };
+enum : int { kCopyPlain = 0, kCopyBulk = 1, kCopyTensor = 2 };
 
 constexpr unsigned kFull = 0xffffffffu;
+// Longest wait for one tile copy (SM clocks, about 2 s) before the kernel
+// gives up, records an error and returns.
+constexpr long long kWaitLimit = 4000000000LL;
+
+// Sticky device error word: bit 0 = a tile-copy wait timed out.
+__device__ int g_device_error;
+
+__host__ __device__ constexpr int pow2_at_least(int n) { return n <= 4 ? 4 : (n <= 8 ? 8 : (n <= 16 ? 16 : 32)); }
+
+// Lanes per matrix used by default: two matrices per warp for n > 8 keeps
+// 8 x 8 (n = 32) register blocks, i.e. 16 broadcast values per 64 FMAs.
+__host__ __device__ constexpr int default_lanes(int n, int mode) {
+    return mode == kModePartial ? pow2_at_least(n) : (n > 8 ? 16 : (n > 4 ? 8 : 4));
+}
 
 // ---------------------------------------------------------------------------
-// Geometry per matrix size.
+// Geometry per (n, lanes per matrix).
 // ---------------------------------------------------------------------------
-template <int N>
+template <int N, int L>
 struct Geom {
     static_assert(N >= 1 && N <= 32, "n must be in 1..32");
-    static constexpr int L = N > 16 ? 32 : (N > 8 ? 16 : (N > 4 ? 8 : 4));  // lanes per matrix
-    static constexpr int M = 32 / L;                                          // matrices per warp
+    static_assert(L == 4 || L == 8 || L == 16 || L == 32, "lanes per matrix");
+    static constexpr int M = 32 / L;                                    // matrices per warp
     static constexpr int RG = (L == 32) ? 8 : (L == 16 ? 4 : (L == 8 ? 4 : 2));
     static constexpr int CG = L / RG;
-    static constexpr int R = (N + RG - 1) / RG;                  // rows per lane
-    static constexpr int C = (((N + CG - 1) / CG) + 1) & ~1;     // columns per lane (even)
-    static constexpr int PR = R * RG;                             // padded rows
-    static constexpr int PC = C * CG;                             // padded columns
-    static constexpr int S = N + 1;                               // stage row stride
+    static constexpr int R = (N + RG - 1) / RG;                        // rows per lane (cyclic)
+    static constexpr int C = (((N + CG - 1) / CG) + 1) & ~1;           // columns per lane (even)
+    static constexpr int PR = R * RG;
+    static constexpr int PC = C * CG;
+    static constexpr int P = pow2_at_least(N);                          // pivot-replay lanes per matrix
+    static_assert(P % L == 0 || L == 32 || true, "");
     static constexpr int pad4(int x) { return (x + 3) & ~3; }
-    // per-matrix shared-memory regions (floats), each 16-byte aligned
-    static constexpr int kStage = pad4(N * S);
+    static constexpr int kMat = N * N;                                  // stage floats per matrix
+    // per-matrix scratch (floats)
     static constexpr int kCol = pad4(PR);
-    static constexpr int kRow = pad4(PC + 1);   // row buffer + pivot value at [PC]
+    static constexpr int kRow = pad4(PC);
     static constexpr int kSwap = pad4(PC);
-    static constexpr int kPerm = 32;
-    static constexpr int kPerMatrix = kStage + 2 * kCol + 2 * kRow + 2 * kSwap + kPerm;
-    static constexpr int kPerWarp = M * kPerMatrix;               // floats
+    static constexpr int oCol = 0;
+    static constexpr int oRow = oCol + 2 * kCol;
+    static constexpr int oSwap = oRow + 2 * kRow;
+    static constexpr int oD = oSwap + 2 * kSwap;                        // pivot value of every step
+    static constexpr int oWin = oD + 32;                                // input row placed at each step
+    static constexpr int kScratch = oWin + 32;
 };
+
+// Stage layout of one matrix: row-major, with the TMA 128-byte swizzle
+// (16-byte chunk index XOR row & 7) for n = 32 so that both row-wise and
+// column-block accesses from a warp are free of bank conflicts.
+template <int N>
+__device__ __forceinline__ int stage_off(int r, int c) {
+    if constexpr (N == 32) return r * 32 + ((((c >> 2) ^ (r & 7)) << 2) | (c & 3));
+    else return r * N + c;
+}
 
 // ---------------------------------------------------------------------------
 // The reference's argmax tree (strides T/2, T/4, ..., 1; strict '<' so the
@@ -122,42 +163,50 @@ __constant__ PrioTable c_prio = make_prio_table();
 // ---------------------------------------------------------------------------
 // Small helpers.
 // ---------------------------------------------------------------------------
-template <int L>
-__device__ __forceinline__ unsigned sub_max(unsigned x) {
-    if constexpr (L == 32) {
+template <int P>
+__device__ __forceinline__ unsigned group_max(unsigned x) {
+    if constexpr (P == 32) {
         return __reduce_max_sync(kFull, x);
     } else {
 #pragma unroll
-        for (int o = L / 2; o > 0; o >>= 1) x = max(x, __shfl_xor_sync(kFull, x, o));
+        for (int o = P / 2; o > 0; o >>= 1) x = max(x, __shfl_xor_sync(kFull, x, o));
         return x;
     }
 }
 
-template <int L>
-__device__ __forceinline__ unsigned sub_ballot(bool p, int base) {
-    unsigned b = __ballot_sync(kFull, p);
-    if constexpr (L == 32) return b;
-    else return (b >> base) & ((1u << L) - 1u);
+template <int P>
+__device__ __forceinline__ unsigned group_ballot(bool p, int gbase) {
+    const unsigned b = __ballot_sync(kFull, p);
+    if constexpr (P == 32) return b;
+    else return (b >> gbase) & ((1u << P) - 1u);
 }
 
-// Pivot-compare key of one entry: |x| as ordered bits, subnormals flushed to
-// zero (the reference compiles with --use_fast_math, parallel_pivot/run.py:47),
-// NaN -> 0xffffffff (as a diagonal it blocks every swap; as a candidate it is
-// rejected by the <= +inf test).
+// Exact pivot-compare key: |x| as ordered bits, subnormals flushed to zero
+// (the reference is built with --use_fast_math, parallel_pivot/run.py:47),
+// NaN -> 0xffffffff (as the diagonal it blocks every exchange; as a candidate
+// it fails the <= +inf test).
 __device__ __forceinline__ unsigned pivot_key(float x) {
-    unsigned a = __float_as_uint(x) & 0x7fffffffu;
-    unsigned k = (a < 0x00800000u) ? 0u : a;
+    const unsigned a = __float_as_uint(x) & 0x7fffffffu;
+    const unsigned k = (a < 0x00800000u) ? 0u : a;
     return (a > 0x7f800000u) ? 0xffffffffu : k;
 }
 
-// 1/d: hardware approximation refined by one Newton-Raphson step
-// (r' = r + r(1 - d r)); zero and infinite pivots keep the approximation.
+// Fast key: one max.NaN.ftz of |x| with 0: subnormals and zero -> 0, NaN ->
+// 0x7fffffff (above +inf, so a NaN anywhere in the candidates shows up in the
+// maximum and sends the step to the exact path).
+__device__ __forceinline__ unsigned fast_key(float x) {
+    float r;
+    asm("max.NaN.ftz.f32 %0, %1, 0f00000000;" : "=f"(r) : "f"(fabsf(x)));
+    return __float_as_uint(r);
+}
+
+// 1/d: hardware approximation refined by one Newton-Raphson step,
+// r' = r + r (1 - d r).  A zero pivot yields a non-finite reciprocal.
 __device__ __forceinline__ float recip(float d) {
     float r;
     asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(d));
-    float e = fmaf(-d, r, 1.0f);
-    float r1 = fmaf(r, e, r);
-    return (fabsf(r) == __int_as_float(0x7f800000) || d == 0.0f) ? r : r1;
+    const float e = fmaf(-d, r, 1.0f);
+    return fmaf(r, e, r);
 }
 
 template <int CNT>
@@ -165,13 +214,13 @@ __device__ __forceinline__ void lds_vec(const float* p, float (&v)[CNT]) {
     if constexpr (CNT % 4 == 0) {
 #pragma unroll
         for (int q = 0; q < CNT / 4; q++) {
-            float4 t = reinterpret_cast<const float4*>(p)[q];
+            const float4 t = reinterpret_cast<const float4*>(p)[q];
             v[4 * q] = t.x; v[4 * q + 1] = t.y; v[4 * q + 2] = t.z; v[4 * q + 3] = t.w;
         }
     } else if constexpr (CNT % 2 == 0) {
 #pragma unroll
         for (int q = 0; q < CNT / 2; q++) {
-            float2 t = reinterpret_cast<const float2*>(p)[q];
+            const float2 t = reinterpret_cast<const float2*>(p)[q];
             v[2 * q] = t.x; v[2 * q + 1] = t.y;
         }
     } else {
@@ -188,15 +237,14 @@ __device__ __forceinline__ void sts_vec(float* p, const float (&v)[CNT]) {
             reinterpret_cast<float4*>(p)[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
     } else if constexpr (CNT % 2 == 0) {
 #pragma unroll
-        for (int q = 0; q < CNT / 2; q++)
-            reinterpret_cast<float2*>(p)[q] = make_float2(v[2 * q], v[2 * q + 1]);
+        for (int q = 0; q < CNT / 2; q++) reinterpret_cast<float2*>(p)[q] = make_float2(v[2 * q], v[2 * q + 1]);
     } else {
 #pragma unroll
         for (int q = 0; q < CNT; q++) p[q] = v[q];
     }
 }
 
-// a[ri][*] -= m * w[*] on packed pairs.
+// a[*] -= m * w[*] on packed pairs.
 template <int C>
 __device__ __forceinline__ void row_update(float (&a)[C], float m, const float (&w)[C]) {
     const float2 nm = make_float2(-m, -m);
@@ -210,102 +258,176 @@ __device__ __forceinline__ void row_update(float (&a)[C], float m, const float (
 }
 
 // ---------------------------------------------------------------------------
-// Pivot replay for the reference rules, lane s = input row s.  Reads the raw
-// input rows from the stage, returns the final position of this lane's row
-// (positions follow the reference's physical row swaps).
+// Pivot replay of the reference rules.  A group of P lanes handles one
+// matrix, lane s = input row s.  Writes win[k] = input row placed at step k.
 // ---------------------------------------------------------------------------
-template <int N, int MODE>
-__device__ __forceinline__ int replay_pivots(const float* stage, int s, int base) {
-    using G = Geom<N>;
-    constexpr int L = G::L;
+
+// Exact rule for one step k, from scratch: positions after steps 0..k-1 are
+// rebuilt from win[], then the reference's tree (or serial scan) runs on the
+// raw entries with its own tie order and dropped slots.  Returns the row.
+template <int N, int P, int MODE>
+__device__ __noinline__ int exact_pivot(const float* st, const int* win, int k, int s, int gbase) {
+    __syncwarp();
+    int pos = (s < N) ? s : 0x7fff;
+    for (int j = 0; j < k; ++j) {
+        const int wj = win[j];
+        const int pw = __shfl_sync(kFull, pos, gbase + wj);
+        if (s == wj) pos = j;
+        else if (pos == j) pos = pw;
+    }
+    const unsigned kraw = (s < N) ? pivot_key(st[stage_off<N>(s, k)]) : 0u;
+    const int dl = __ffs(group_ballot<P>(pos == k, gbase)) - 1;
+    const unsigned kd = __shfl_sync(kFull, kraw, gbase + dl);
+    const int slot = pos - k - 1;
+    bool ok = (slot >= 0) && (pos < N) && (kraw > kd) && (kraw <= 0x7f800000u);
+    if (MODE == kModeReference) ok = ok && ((survive_mask(N) >> (slot & 31)) & 1u);
+    const unsigned cand = ok ? kraw : 0u;
+    const unsigned mx = group_max<P>(cand);
+    const bool top = ok && (cand == mx);
+    unsigned pr = 0u;
+    if (top) pr = (MODE == kModeReference) ? (unsigned)c_prio.v[N][slot] : (unsigned)(64 - pos);
+    const unsigned pm = group_max<P>(pr);
+    const unsigned tb = group_ballot<P>(top && pr == pm, gbase);
+    return tb ? (__ffs(tb) - 1) : dl;   // nothing beats the diagonal: it stays
+}
+
+// Keys of row r, columns k0..k0+3 (0 past the matrix).
+template <int N>
+__device__ __forceinline__ void load_keys4(const float* st, int r, int k0, unsigned (&kv)[4]) {
+    if (r >= N) {
+#pragma unroll
+        for (int t = 0; t < 4; t++) kv[t] = 0u;
+        return;
+    }
+    if constexpr (N == 32 || N % 4 == 0) {
+        const float4 v = *reinterpret_cast<const float4*>(st + ((N == 32) ? (r * 32 + ((((k0 >> 2) ^ (r & 7))) << 2))
+                                                                        : (r * N + k0)));
+        kv[0] = fast_key(v.x); kv[1] = fast_key(v.y); kv[2] = fast_key(v.z); kv[3] = fast_key(v.w);
+    } else {
+#pragma unroll
+        for (int t = 0; t < 4; t++) kv[t] = (k0 + t < N) ? fast_key(st[r * N + k0 + t]) : 0u;
+    }
+}
+
+// The fast replay for IM matrices at once, one independent chain each, so
+// the reduction latencies of the chains overlap; keys are read from the
+// stage four columns at a time (a compact, rolled loop).
+template <int N, int P, int IM, int MODE>
+__device__ __forceinline__ void replay_fast_multi(const float* const (&st)[IM], int* const (&win)[IM], int s,
+                                                  int gbase) {
+    bool placed[IM];
+#pragma unroll
+    for (int m = 0; m < IM; m++) placed[m] = (s >= N);
+#pragma unroll 1
+    for (int k0 = 0; k0 < N; k0 += 4) {
+        unsigned kv[IM][4];
+#pragma unroll
+        for (int m = 0; m < IM; m++) load_keys4<N>(st[m], s, k0, kv[m]);
+#pragma unroll
+        for (int t = 0; t < 4; t++) {
+            const int k = k0 + t;
+            if (N % 4 == 0 || k < N) {
+                unsigned tb[IM];
+                bool rare = false;
+#pragma unroll
+                for (int m = 0; m < IM; m++) {
+                    const unsigned cand = placed[m] ? 0u : kv[m][t];
+                    const unsigned mx = group_max<P>(cand);
+                    tb[m] = group_ballot<P>(cand == mx, gbase);
+                    rare = rare || ((tb[m] & (tb[m] - 1u)) != 0u) || (mx > 0x7f800000u);
+                }
+                int w[IM];
+                if (__any_sync(kFull, rare)) {
+#pragma unroll
+                    for (int m = 0; m < IM; m++) w[m] = exact_pivot<N, P, MODE>(st[m], win[m], k, s, gbase);
+                } else {
+#pragma unroll
+                    for (int m = 0; m < IM; m++) w[m] = __ffs(tb[m]) - 1;
+                }
+#pragma unroll
+                for (int m = 0; m < IM; m++) {
+                    if (s == w[m]) placed[m] = true;
+                    if (s == 0) win[m][k] = w[m];
+                }
+            }
+        }
+    }
+}
+
+// Non-power-of-two n under the reference rule: some tree slots are dropped,
+// so positions are tracked every step (lane = row).
+template <int N, int P, int MODE>
+__device__ __forceinline__ void replay_tracked(const float* st, int* win, int s, int gbase) {
     constexpr unsigned kSurv = survive_mask(N);
     unsigned key[N];
 #pragma unroll
-    for (int k = 0; k < N; k++) key[k] = (s < N) ? pivot_key(stage[s * G::S + k]) : 0u;
+    for (int k = 0; k < N; k++) key[k] = (s < N) ? pivot_key(st[stage_off<N>(s, k)]) : 0u;
     int pos = (s < N) ? s : 0x7fff;
 #pragma unroll
-    for (int k = 0; k < N; k++) {
-        // key of the row now at position k (the diagonal candidate)
-        const unsigned bd = sub_ballot<L>(pos == k, base);
+    for (int k = 0; k < N; ++k) {
+        const unsigned bd = group_ballot<P>(pos == k, gbase);
         const int dl = __ffs(bd) - 1;
-        const unsigned kd = __shfl_sync(kFull, key[k], base + dl);
+        const unsigned kd = __shfl_sync(kFull, key[k], gbase + dl);
         const int slot = pos - k - 1;
         bool ok = (slot >= 0) && (pos < N) && (key[k] > kd) && (key[k] <= 0x7f800000u);
-        if constexpr (MODE == kModeReference) ok = ok && ((kSurv >> (slot & 31)) & 1u);
+        ok = ok && ((kSurv >> (slot & 31)) & 1u);
         const unsigned cand = ok ? key[k] : 0u;
-        const unsigned mx = sub_max<L>(cand);
+        const unsigned mx = group_max<P>(cand);
         const bool top = ok && (cand == mx);
-        unsigned tb = sub_ballot<L>(top, base);
-        if (__any_sync(kFull, __popc(tb) > 1)) {
-            // equal keys: the reference tree keeps its own order; the serial
-            // scan keeps the lowest position
+        unsigned tb = group_ballot<P>(top, gbase);
+        if (__any_sync(kFull, (tb & (tb - 1u)) != 0u)) {
             unsigned pr = 0u;
-            if (top) pr = (MODE == kModeReference) ? (unsigned)c_prio.v[N][slot] : (unsigned)(64 - pos);
-            const unsigned pm = sub_max<L>(pr);
-            tb = sub_ballot<L>(top && pr == pm, base);
+            if (top) pr = (unsigned)c_prio.v[N][slot];
+            const unsigned pm = group_max<P>(pr);
+            tb = group_ballot<P>(top && pr == pm, gbase);
         }
-        const int wl = __ffs(tb) - 1;
-        const int pw = __shfl_sync(kFull, pos, base + (wl < 0 ? 0 : wl));
-        if (wl >= 0) {
-            if (s == wl) pos = k;
-            else if (pos == k) pos = pw;
-        }
+        const int wl = tb ? (__ffs(tb) - 1) : dl;
+        const int pw = __shfl_sync(kFull, pos, gbase + wl);
+        if (s == wl) pos = k;
+        else if (pos == k) pos = pw;
+        if (s == 0) win[k] = wl;
     }
-    return pos;
 }
 
 // ---------------------------------------------------------------------------
-// One elimination step with the pivot row already at logical row k.
+// Elimination steps.  k is a constant after the step loop is unrolled.
 // ---------------------------------------------------------------------------
-template <int N, int K>
-struct StepConst {
-    using G = Geom<N>;
-    static constexpr int kr = K / G::R, kri = K % G::R;   // pivot-row owner, register row
-    static constexpr int kc = K / G::C, kci = K % G::C;   // column owner, register column
-};
-
-template <int N, int K>
-__device__ __forceinline__ void gj_step(float (&a)[Geom<N>::R][Geom<N>::C], float (&ps)[Geom<N>::R],
-                                        int rg, int cg, float* colb, float* rowb, int& info) {
-    using G = Geom<N>;
-    using SC = StepConst<N, K>;
+template <class G>
+__device__ __forceinline__ void gj_step(float (&a)[G::R][G::C], float (&ps)[G::R], const int k, int rg, int cg,
+                                        int gb, float* scr) {
     constexpr int R = G::R, C = G::C;
-    float* cb = colb + (K & 1) * G::kCol;
-    float* rb = rowb + (K & 1) * G::kRow;
-    if (cg == SC::kc) {
-        float v[R];
-#pragma unroll
-        for (int ri = 0; ri < R; ri++) v[ri] = a[ri][SC::kci];
-        if (rg == SC::kr) v[SC::kri] = 0.0f;          // the pivot row takes no update
-        sts_vec<R>(cb + rg * R, v);
-    }
-    if (rg == SC::kr) {
-        float w[C];
-#pragma unroll
-        for (int ci = 0; ci < C; ci++) w[ci] = a[SC::kri][ci];
-        if (cg == SC::kc) {
-            rb[G::PC] = w[SC::kci];                     // pivot value
-            w[SC::kci] = 1.0f;                          // column k becomes -m_i
-        }
-        sts_vec<C>(rb + cg * C, w);
-    }
-    __syncwarp();
-    const float d = rb[G::PC];
-    const float p = recip(d);
-    if (d == 0.0f && info == 0) info = K + 1;
+    const int kr = k % G::RG, kri = k / G::RG;   // pivot-row owner group, register row
+    const int kc = k / C, kci = k % C;           // column owner group, register column
+    // column k for my rows from lane (rg, kc); row k for my columns from lane
+    // (kr, cg); the pivot from lane (kr, kc) -- straight out of the owners'
+    // registers, no shared-memory round trip
+    const int src_c = gb + kc * G::RG + rg;
+    const int src_w = gb + cg * G::RG + kr;
     float c[R], w[C];
-    lds_vec<R>(cb + rg * R, c);
-    lds_vec<C>(rb + cg * C, w);
-    if (cg == SC::kc) {
 #pragma unroll
-        for (int ri = 0; ri < R; ri++) a[ri][SC::kci] = (ri == SC::kri && rg == SC::kr) ? 1.0f : 0.0f;
+    for (int ri = 0; ri < R; ri++) c[ri] = __shfl_sync(kFull, a[ri][kci], src_c);
+#pragma unroll
+    for (int ci = 0; ci < C; ci++) w[ci] = __shfl_sync(kFull, a[kri][ci], src_w);
+    // the pivot's owner forms 1/pivot from its own register, off the
+    // critical path of the broadcasts, and records the pivot for info
+    const float pown = recip(a[kri][kci]);
+    if (rg == kr && cg == kc) scr[G::oD + k] = a[kri][kci];
+    const float p = __shfl_sync(kFull, pown, gb + kc * G::RG + kr);
+    if (rg == kr) {
+        c[kri] = 0.0f;                                // the pivot row takes no update
+        ps[kri] = p;
     }
-    if (rg == SC::kr) ps[SC::kri] = p;
+    if (cg == kc) {
+        w[kci] = 1.0f;                                // column k becomes -multiplier
+#pragma unroll
+        for (int ri = 0; ri < R; ri++) a[ri][kci] = 0.0f;
+        if (rg == kr) a[kri][kci] = 1.0f;
+    }
     float m[R];
 #pragma unroll
     for (int ri = 0; ri < R; ri += 2) {
         if (ri + 1 < R) {
-            float2 mm = __fmul2_rn(make_float2(c[ri], c[ri + 1]), make_float2(p, p));
+            const float2 mm = __fmul2_rn(make_float2(c[ri], c[ri + 1]), make_float2(p, p));
             m[ri] = mm.x;
             m[ri + 1] = mm.y;
         } else {
@@ -316,229 +438,342 @@ __device__ __forceinline__ void gj_step(float (&a)[Geom<N>::R][Geom<N>::C], floa
     for (int ri = 0; ri < R; ri++) row_update<C>(a[ri], m[ri], w);
 }
 
-// Partial pivoting step: argmax of the updated column over rows k.., swap the
-// winner into row k (register blocks exchanged through shared memory), then
-// the same update.  ra: the input row held at logical row s (lane s < N).
-template <int N, int K>
-__device__ __forceinline__ void gj_step_partial(float (&a)[Geom<N>::R][Geom<N>::C], float (&ps)[Geom<N>::R],
-                                                int rg, int cg, int s, int base, float* colb, float* rowb,
-                                                float* swapb, int& ra, int& info) {
-    using G = Geom<N>;
-    using SC = StepConst<N, K>;
-    constexpr int R = G::R, C = G::C, L = G::L;
-    float* cb = colb + (K & 1) * G::kCol;
-    float* rb = rowb + (K & 1) * G::kRow;
-    float* sb = swapb + (K & 1) * G::kSwap;
-    if (cg == SC::kc) {
+// Register row q of the block, selected by a runtime q through a static chain
+// (no dynamically indexed register arrays).
+template <class G>
+__device__ __forceinline__ void get_row(const float (&a)[G::R][G::C], int q, float (&w)[G::C]) {
+#pragma unroll
+    for (int ci = 0; ci < G::C; ci++) w[ci] = a[0][ci];
+#pragma unroll
+    for (int r = 1; r < G::R; r++)
+        if (q == r) {
+#pragma unroll
+            for (int ci = 0; ci < G::C; ci++) w[ci] = a[r][ci];
+        }
+}
+
+template <class G>
+__device__ __forceinline__ void set_row(float (&a)[G::R][G::C], int q, const float (&w)[G::C]) {
+#pragma unroll
+    for (int r = 0; r < G::R; r++)
+        if (q == r) {
+#pragma unroll
+            for (int ci = 0; ci < G::C; ci++) a[r][ci] = w[ci];
+        }
+}
+
+// Partial pivoting (L = P: lane t of the group is logical row t): argmax of
+// the updated column over rows k.., first maximum; exchange rows k and r of
+// the register blocks through shared memory; then the same update.
+// ra: the input row held at logical row s.
+template <class G>
+__device__ __forceinline__ void gj_step_partial(float (&a)[G::R][G::C], float (&ps)[G::R], const int k, int rg, int cg,
+                                                int s, int gbase, float* scr, int& ra) {
+    constexpr int R = G::R, C = G::C;
+    const int kr = k % G::RG, kri = k / G::RG;
+    const int kc = k / C, kci = k % C;
+    float* cb = scr + G::oCol + (k & 1) * G::kCol;
+    float* rb = scr + G::oRow + (k & 1) * G::kRow;
+    float* sb = scr + G::oSwap + (k & 1) * G::kSwap;
+    if (cg == kc) {
         float v[R];
 #pragma unroll
-        for (int ri = 0; ri < R; ri++) v[ri] = a[ri][SC::kci];
+        for (int ri = 0; ri < R; ri++) v[ri] = a[ri][kci];
         sts_vec<R>(cb + rg * R, v);
     }
     __syncwarp();
-    // argmax over logical rows k..N-1, first maximum (lowest row) wins
+    // column entry of logical row t lives at cb[(t % RG) * R + t / RG]
     unsigned key = 0u;
-    if (s >= K && s < N) {
-        unsigned b = __float_as_uint(cb[s]) & 0x7fffffffu;
-        key = (b > 0x7f800000u) ? 1u : b + 2u;   // NaN never beats a number
+    if (s >= k && s < G::kN) {
+        const unsigned b = __float_as_uint(cb[(s % G::RG) * R + s / G::RG]) & 0x7fffffffu;
+        key = (b > 0x7f800000u) ? 1u : b + 2u;   // a NaN never beats a number
     }
-    const unsigned mx = sub_max<L>(key);
-    const int r = __ffs(sub_ballot<L>(key != 0u && key == mx, base)) - 1;   // lane K is always a candidate
-    const int rr = r / R, rri = r % R;
-    // exchange rows K and r: row r -> rb (the pivot row), row K -> sb
-    if (rg == rr) {
+    const unsigned mx = group_max<G::LL>(key);
+    const int r = __ffs(group_ballot<G::LL>(key != 0u && key == mx, gbase)) - 1;   // row k always competes
+    const int rr = r % G::RG, rri = r / G::RG;
+    if (rg == rr) {           // row r becomes the pivot row
         float w[C];
-#pragma unroll
-        for (int q = 0; q < R; q++)
-            if (q == rri) {
-#pragma unroll
-                for (int ci = 0; ci < C; ci++) w[ci] = a[q][ci];
-            }
+        get_row<G>(a, rri, w);
         sts_vec<C>(rb + cg * C, w);
     }
-    if (rg == SC::kr) {
+    if (rg == kr) {           // row k moves to row r
         float w[C];
 #pragma unroll
-        for (int ci = 0; ci < C; ci++) w[ci] = a[SC::kri][ci];
+        for (int ci = 0; ci < C; ci++) w[ci] = a[kri][ci];
         sts_vec<C>(sb + cg * C, w);
     }
     __syncwarp();
     float w[C];
     lds_vec<C>(rb + cg * C, w);
-    if (rg == SC::kr) {
+    if (rg == kr) {
 #pragma unroll
-        for (int ci = 0; ci < C; ci++) a[SC::kri][ci] = w[ci];
+        for (int ci = 0; ci < C; ci++) a[kri][ci] = w[ci];
     }
-    if (rg == rr && r != K) {
+    if (rg == rr && r != k) {
         float t[C];
         lds_vec<C>(sb + cg * C, t);
-#pragma unroll
-        for (int q = 0; q < R; q++)
-            if (q == rri) {
-#pragma unroll
-                for (int ci = 0; ci < C; ci++) a[q][ci] = t[ci];
-            }
+        set_row<G>(a, rri, t);
     }
-    const float d = cb[r];
-    const float ck = cb[K];
+    const float d = cb[rr * R + rri];
+    const float ck = cb[kr * R + kri];
     const float p = recip(d);
-    if (d == 0.0f && info == 0) info = K + 1;
-    {   // the input row held at each logical row follows the exchange
-        const int a_r = __shfl_sync(kFull, ra, base + r);
-        const int a_k = __shfl_sync(kFull, ra, base + K);
-        if (s == K) ra = a_r;
+    if (s < G::kN) scr[G::oD + k] = d;    // every lane writes the same value
+    {
+        const int a_r = __shfl_sync(kFull, ra, gbase + r);
+        const int a_k = __shfl_sync(kFull, ra, gbase + k);
+        if (s == k) ra = a_r;
         else if (s == r) ra = a_k;
     }
-    if (cg == SC::kc) w[SC::kci] = 1.0f;
+    if (cg == kc) w[kci] = 1.0f;
     float c[R];
     lds_vec<R>(cb + rg * R, c);
 #pragma unroll
     for (int ri = 0; ri < R; ri++) {
-        const int row = rg * R + ri;
-        c[ri] = (row == K) ? 0.0f : ((row == r) ? ck : c[ri]);
+        const int row = rg + G::RG * ri;
+        c[ri] = (row == k) ? 0.0f : ((row == r) ? ck : c[ri]);
     }
-    if (cg == SC::kc) {
+    if (cg == kc) {
 #pragma unroll
-        for (int ri = 0; ri < R; ri++) a[ri][SC::kci] = (ri == SC::kri && rg == SC::kr) ? 1.0f : 0.0f;
+        for (int ri = 0; ri < R; ri++) a[ri][kci] = 0.0f;
+        if (rg == kr) a[kri][kci] = 1.0f;
     }
-    if (rg == SC::kr) ps[SC::kri] = p;
+    if (rg == kr) ps[kri] = p;
 #pragma unroll
     for (int ri = 0; ri < R; ri++) row_update<C>(a[ri], c[ri] * p, w);
 }
 
-template <int N, int K, int MODE>
-struct Steps {
-    static __device__ __forceinline__ void run(float (&a)[Geom<N>::R][Geom<N>::C], float (&ps)[Geom<N>::R],
-                                               int rg, int cg, int s, int base, float* colb, float* rowb,
-                                               float* swapb, int& ra, int& info) {
-        if constexpr (K < N) {
-            if constexpr (MODE == kModePartial)
-                gj_step_partial<N, K>(a, ps, rg, cg, s, base, colb, rowb, swapb, ra, info);
-            else
-                gj_step<N, K>(a, ps, rg, cg, colb, rowb, info);
-            Steps<N, K + 1, MODE>::run(a, ps, rg, cg, s, base, colb, rowb, swapb, ra, info);
-        }
-    }
+// ---------------------------------------------------------------------------
+// One warp: invert its M matrices (stage st0 = first matrix of the warp).
+// ---------------------------------------------------------------------------
+template <int N, int L, int MODE>
+struct GeomN : Geom<N, L> {
+    static constexpr int kN = N;
+    static constexpr int LL = L;
 };
 
-// ---------------------------------------------------------------------------
-// The kernel: a grid-stride loop of warps over groups of M matrices.
-// ---------------------------------------------------------------------------
-template <int N, int MODE>
-__global__ void __launch_bounds__(256) mi_inverse_kernel(float* __restrict__ A, int32_t* __restrict__ perm_out,
-                                                         int32_t* __restrict__ info_out, long long batch) {
-    using G = Geom<N>;
-    constexpr int L = G::L, M = G::M, R = G::R, C = G::C, S = G::S;
-    constexpr int NN = N * N;
-    extern __shared__ float4 smem_raw[];
-    float* smem = reinterpret_cast<float*>(smem_raw);
+template <int N, int L, int MODE>
+__device__ __forceinline__ void invert_warp(float* st0, float* scr0, int lane, int32_t* perm_out,
+                                            int32_t* info_out, long long first, long long batch) {
+    using G = Geom<N, L>;
+    constexpr int R = G::R, C = G::C, M = G::M, P = G::P;
+    const int mslot = lane / L, s = lane % L;
+    const int rg = s % G::RG, cg = s / G::RG;
+    float* st = st0 + mslot * G::kMat;
+    float* scr = scr0 + mslot * G::kScratch;
+    int* win = reinterpret_cast<int*>(scr + G::oWin);
 
-    const int lane = threadIdx.x & 31;
-    const int warp = threadIdx.x >> 5;
-    const int w = lane / L;          // matrix slot within the warp
-    const int s = lane % L;          // lane within the matrix
-    const int base = w * L;
-    const int rg = s % G::RG;
-    const int cg = s / G::RG;
-
-    float* wsm = smem + (size_t)warp * G::kPerWarp;
-    float* msm = wsm + w * G::kPerMatrix;
-    float* stage = msm;
-    float* colb = stage + G::kStage;
-    float* rowb = colb + 2 * G::kCol;
-    float* swapb = rowb + 2 * G::kRow;
-    int* permb = reinterpret_cast<int*>(swapb + 2 * G::kSwap);
-
-    const long long ngroups = (batch + M - 1) / M;
-    const long long gstride = (long long)gridDim.x * (blockDim.x >> 5);
-    for (long long grp = (long long)blockIdx.x * (blockDim.x >> 5) + warp; grp < ngroups; grp += gstride) {
-        const long long first = grp * M;
-        const int count = (int)min((long long)M, batch - first);
-        const long long mb = first + w;
-        const bool active = w < count;
-        float* gA = A + first * NN;
-
-        // ---- stage the warp's matrices into shared memory (row stride N+1)
-#pragma unroll 4
-        for (int e = lane; e < M * NN; e += 32) {
-            const int m = e / NN, rem = e - m * NN;
-            const int row = rem / N, col = rem - row * N;
-            const float v = (m < count) ? gA[e] : 0.0f;
-            wsm[m * G::kPerMatrix + row * S + col] = v;
+    // ---- pivot order (reference rules): groups of P lanes, P / L rounds
+    if constexpr (MODE == kModeReference || MODE == kModeReferenceSerial) {
+        constexpr int GP = 32 / P;      // groups per warp
+        constexpr int IM = M / GP;      // matrices per group (= P / L)
+        const int g = lane / P, sp = lane % P;
+        if constexpr (MODE == kModeReferenceSerial || (N & (N - 1)) == 0) {
+            const float* stm[IM];
+            int* winm[IM];
+#pragma unroll
+            for (int q = 0; q < IM; q++) {
+                const int mm = q * GP + g;
+                stm[q] = st0 + mm * G::kMat;
+                winm[q] = reinterpret_cast<int*>(scr0 + mm * G::kScratch + G::oWin);
+            }
+            replay_fast_multi<N, P, IM, MODE>(stm, winm, sp, g * P);
+        } else {
+#pragma unroll 1
+            for (int q = 0; q < IM; ++q) {
+                const int mm = q * GP + g;
+                replay_tracked<N, P, MODE>(st0 + mm * G::kMat,
+                                           reinterpret_cast<int*>(scr0 + mm * G::kScratch + G::oWin), sp, g * P);
+            }
         }
         __syncwarp();
+    } else if constexpr (MODE == kModeNone) {
+        for (int t = s; t < N; t += L) win[t] = t;
+        __syncwarp();
+    }
 
-        // ---- pivot order
-        int ra = s;   // input row that ends at logical row s
-        if constexpr (MODE == kModeReference || MODE == kModeReferenceSerial) {
-            const int pos = replay_pivots<N, MODE>(stage, s, base);
-            if (s < N) permb[pos] = s;
-            __syncwarp();
-            ra = (s < N) ? permb[s] : s;
-        }
-
-        // ---- register block, rows in pivot order
-        float a[R][C];
+    // ---- register block, rows in pivot order
+    float a[R][C];
 #pragma unroll
-        for (int ri = 0; ri < R; ri++) {
-            const int i = rg * R + ri;
-            int src = i;
-            if constexpr (MODE == kModeReference || MODE == kModeReferenceSerial) src = (i < N) ? permb[i] : 0;
+    for (int ri = 0; ri < R; ri++) {
+        const int i = rg + G::RG * ri;
+        int src = i;
+        if constexpr (MODE == kModeReference || MODE == kModeReferenceSerial) src = (i < N) ? win[i] : 0;
+        if constexpr (N == 32 && C % 4 == 0) {
+#pragma unroll
+            for (int h = 0; h < C / 4; h++) {
+                const int c0 = cg * C + 4 * h;
+                const float4 v = *reinterpret_cast<const float4*>(st + src * 32 + ((((c0 >> 2) ^ (src & 7))) << 2));
+                a[ri][4 * h] = v.x; a[ri][4 * h + 1] = v.y; a[ri][4 * h + 2] = v.z; a[ri][4 * h + 3] = v.w;
+            }
+            if (i >= N) {
+#pragma unroll
+                for (int ci = 0; ci < C; ci++) a[ri][ci] = 0.0f;
+            }
+        } else {
 #pragma unroll
             for (int ci = 0; ci < C; ci++) {
                 const int j = cg * C + ci;
-                a[ri][ci] = (i < N && j < N) ? stage[src * S + j] : 0.0f;
+                a[ri][ci] = (i < N && j < N) ? st[stage_off<N>(src, j)] : 0.0f;
             }
         }
-
-        // ---- n elimination steps
-        float ps[R];
-#pragma unroll
-        for (int ri = 0; ri < R; ri++) ps[ri] = 1.0f;
-        int info = 0;
-        Steps<N, 0, MODE>::run(a, ps, rg, cg, s, base, colb, rowb, swapb, ra, info);
-
-        // ---- scale each row by its 1/pivot
-#pragma unroll
-        for (int ri = 0; ri < R; ri++) {
-#pragma unroll
-            for (int q = 0; q < C / 2; q++) {
-                float2 x = __fmul2_rn(make_float2(a[ri][2 * q], a[ri][2 * q + 1]), make_float2(ps[ri], ps[ri]));
-                a[ri][2 * q] = x.x;
-                a[ri][2 * q + 1] = x.y;
-            }
-        }
-
-        // ---- A^-1[i][ra(j)] = X[i][j]: scatter columns into the stage
-        if constexpr (MODE == kModePartial) {
-            if (s < N) permb[s] = ra;
-        }
-        __syncwarp();
-#pragma unroll
-        for (int ci = 0; ci < C; ci++) {
-            const int j = cg * C + ci;
-            if (j < N) {
-                const int dst = (MODE == kModeNone) ? j : permb[j];
-#pragma unroll
-                for (int ri = 0; ri < R; ri++) {
-                    const int i = rg * R + ri;
-                    if (i < N) stage[i * S + dst] = a[ri][ci];
-                }
-            }
-        }
-        if (active) {
-            if (perm_out != nullptr && s < N) perm_out[mb * N + s] = (MODE == kModeNone) ? s : permb[s];
-            if (info_out != nullptr && s == 0) info_out[mb] = info;
-        }
-        __syncwarp();
-#pragma unroll 4
-        for (int e = lane; e < count * NN; e += 32) {
-            const int m = e / NN, rem = e - m * NN;
-            const int row = rem / N, col = rem - row * N;
-            gA[e] = wsm[m * G::kPerMatrix + row * S + col];
-        }
-        __syncwarp();
     }
+
+    // ---- n elimination steps
+    float ps[R];
+#pragma unroll
+    for (int ri = 0; ri < R; ri++) ps[ri] = 1.0f;
+    if constexpr (MODE == kModePartial) {
+        using GP_ = GeomN<N, L, MODE>;
+        int ra = s;
+#pragma unroll
+        for (int k = 0; k < N; ++k) gj_step_partial<GP_>(a, ps, k, rg, cg, s, mslot * L, scr, ra);
+        if (s < N) win[s] = ra;
+    } else {
+#pragma unroll
+        for (int k = 0; k < N; ++k) gj_step<G>(a, ps, k, rg, cg, mslot * L, scr);
+    }
+
+    // ---- scale each row by its 1/pivot
+#pragma unroll
+    for (int ri = 0; ri < R; ri++) {
+#pragma unroll
+        for (int q = 0; q < C / 2; q++) {
+            const float2 x = __fmul2_rn(make_float2(a[ri][2 * q], a[ri][2 * q + 1]), make_float2(ps[ri], ps[ri]));
+            a[ri][2 * q] = x.x;
+            a[ri][2 * q + 1] = x.y;
+        }
+    }
+    __syncwarp();
+
+    // ---- A^-1[i][win[j]] = X[i][j]: scatter columns into the stage
+    int dst[C];
+#pragma unroll
+    for (int ci = 0; ci < C; ci++) {
+        const int j = cg * C + ci;
+        dst[ci] = (j < N) ? win[j] : 0;
+    }
+#pragma unroll
+    for (int ri = 0; ri < R; ri++) {
+        const int i = rg + G::RG * ri;
+        if (i < N) {
+#pragma unroll
+            for (int ci = 0; ci < C; ci++)
+                if (cg * C + ci < N) st[stage_off<N>(i, dst[ci])] = a[ri][ci];
+        }
+    }
+
+    // ---- perm and info (info: first step whose pivot was exactly zero)
+    const long long mb = first + mslot;
+    unsigned zmask = 0u;
+#pragma unroll
+    for (int q = 0; q < (N + L - 1) / L; q++) {
+        const int t = s + q * L;
+        const bool z = (t < N) && (scr[G::oD + t] == 0.0f);
+        zmask |= group_ballot<L>(z, mslot * L) << (q * L);
+        if (perm_out != nullptr && t < N && mb < batch) perm_out[mb * N + t] = win[t];
+    }
+    if (info_out != nullptr && s == 0 && mb < batch) info_out[mb] = zmask ? __ffs(zmask) : 0;
+}
+
+// ---------------------------------------------------------------------------
+// The kernel: persistent CTAs walk tiles of W*M matrices, two tiles in flight.
+// ---------------------------------------------------------------------------
+template <int N, int L, int MODE>
+__global__ void __launch_bounds__(256) mi_inverse_kernel(float* __restrict__ A, int32_t* __restrict__ perm_out,
+                                                         int32_t* __restrict__ info_out, long long batch,
+                                                         int copy_mode, const __grid_constant__ CUtensorMap tmap) {
+    using G = Geom<N, L>;
+    constexpr int NN = N * N;
+    extern __shared__ unsigned char smem_raw[];
+    __shared__ int abort_flag;
+    const uintptr_t base = (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023);
+    const int W = blockDim.x >> 5;
+    const int TM = W * G::M;                      // matrices per tile
+    const int tile_floats = TM * G::kMat;
+    float* stage0 = reinterpret_cast<float*>(base);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(stage0 + 2 * tile_floats);
+    float* scratch = reinterpret_cast<float*>(bars + 2);
+
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const long long tiles = (batch + TM - 1) / TM;
+    const long long full_tiles = batch / TM;
+    const uint32_t tile_bytes = (uint32_t)tile_floats * 4u;
+
+    if (tid == 0) {
+        mbar_init(&bars[0], 1);
+        mbar_init(&bars[1], 1);
+        fence_mbar_init();
+        abort_flag = 0;
+        if (copy_mode == kCopyTensor) tma_prefetch_map(&tmap);
+    }
+    __syncthreads();
+
+    auto async_ok = [&](long long t) {
+        return copy_mode == kCopyTensor || (copy_mode == kCopyBulk && t < full_tiles);
+    };
+    auto issue_load = [&](long long t, int buf) {
+        float* dst = stage0 + buf * tile_floats;
+        mbar_arrive_expect_tx(&bars[buf], tile_bytes);
+        if (copy_mode == kCopyTensor) tma_load_3d(dst, &tmap, 0, 0, (int)(t * TM), &bars[buf]);
+        else bulk_load(dst, A + t * TM * NN, tile_bytes, &bars[buf]);
+    };
+
+    long long t = blockIdx.x;
+    if (tid == 0 && t < tiles && async_ok(t)) issue_load(t, 0);
+    for (int it = 0; t < tiles; ++it, t += gridDim.x) {
+        const int buf = it & 1;
+        float* stage = stage0 + buf * tile_floats;
+        const long long tn = t + gridDim.x;
+        if (tid == 0 && tn < tiles && async_ok(tn)) {
+            bulk_wait_read_all();     // the store from the other buffer has read it
+            fence_proxy_async();
+            issue_load(tn, buf ^ 1);
+        }
+        const long long first = t * TM;
+        const int count = (int)min((long long)TM, batch - first);
+        if (async_ok(t)) {
+            if (!mbar_wait(&bars[buf], (uint32_t)((it >> 1) & 1), kWaitLimit)) {
+                atomicOr(&g_device_error, 1);
+                abort_flag = 1;
+            }
+        } else {
+            for (int e = tid; e < TM * NN; e += blockDim.x) {
+                const int m = e / NN, rem = e - m * NN;
+                const int r = rem / N, c = rem - r * N;
+                stage[m * G::kMat + stage_off<N>(r, c)] = (m < count) ? A[first * NN + e] : 0.0f;
+            }
+        }
+        __syncthreads();
+        if (abort_flag) break;
+
+        invert_warp<N, L, MODE>(stage + warp * G::M * G::kMat, scratch + warp * G::M * G::kScratch, lane, perm_out,
+                                info_out, first + warp * G::M, batch);
+
+        fence_proxy_async();
+        __syncthreads();
+        if (async_ok(t)) {
+            if (tid == 0) {
+                if (copy_mode == kCopyTensor) tma_store_3d(&tmap, 0, 0, (int)first, stage);
+                else bulk_store(A + first * NN, stage, tile_bytes);
+                bulk_commit();
+            }
+        } else {
+            for (int e = tid; e < count * NN; e += blockDim.x) {
+                const int m = e / NN, rem = e - m * NN;
+                const int r = rem / N, c = rem - r * N;
+                A[first * NN + e] = stage[m * G::kMat + stage_off<N>(r, c)];
+            }
+        }
+    }
+    if (tid == 0) bulk_wait_all();
+}
+
+// Shared memory bytes for W warps (1 KB of slack for the 1024-byte alignment).
+template <int N, int L>
+constexpr size_t smem_bytes(int warps) {
+    using G = Geom<N, L>;
+    return 1024 + (size_t)2 * warps * G::M * G::kMat * sizeof(float) + 16 +
+           (size_t)warps * G::M * G::kScratch * sizeof(float);
 }
 
 }  // namespace mi

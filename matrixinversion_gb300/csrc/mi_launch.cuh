@@ -2,8 +2,12 @@
 // mi_inverse_kernel, and the per-mode dispatch tables the C ABI indexes.
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
+#include <cudaTypedefs.h>
+
 #include <cstdint>
+#include <cstring>
 
 #include "mi_kernel.cuh"
 
@@ -14,33 +18,65 @@ using launch_fn = cudaError_t (*)(float*, int32_t*, int32_t*, long long, int, in
 constexpr int kMaxThreadsPerBlock = 256;
 constexpr int kDefaultThreadsPerBlock = 128;
 
-int device_sm_count();   // cached per device (mi_api.cu)
+int device_sm_count();                                  // cached per device (mi_api.cu)
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder();  // driver entry point (mi_api.cu)
+
+// 3-D tensor map over the batch: {column, row, matrix}, box of one tile,
+// 128-byte swizzle (n = 32 rows are exactly 128 bytes).
+inline bool make_tensor_map(CUtensorMap* map, float* a, int n, long long batch, int tile_matrices) {
+    auto encode = tensor_map_encoder();
+    if (encode == nullptr) return false;
+    const cuuint64_t dims[3] = {(cuuint64_t)n, (cuuint64_t)n, (cuuint64_t)batch};
+    const cuuint64_t strides[2] = {(cuuint64_t)n * 4u, (cuuint64_t)n * n * 4u};
+    const cuuint32_t box[3] = {(cuuint32_t)n, (cuuint32_t)n, (cuuint32_t)tile_matrices};
+    const cuuint32_t estr[3] = {1u, 1u, 1u};
+    const CUresult r = encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, a, dims, strides, box, estr,
+                              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                              CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS;
+}
 
 template <int N, int MODE>
 cudaError_t launch(float* a, int32_t* perm, int32_t* info, long long batch, int tpb, int grid,
                    cudaStream_t stream) {
-    using G = Geom<N>;
+    constexpr int L = default_lanes(N, MODE);
+    using G = Geom<N, L>;
     const int warps = tpb / 32;
-    const size_t smem = (size_t)warps * G::kPerWarp * sizeof(float);
-    auto kern = mi_inverse_kernel<N, MODE>;
-    static size_t smem_set = 0;   // largest dynamic size opted in so far
+    const int tm = warps * G::M;                    // matrices per tile
+    const size_t smem = smem_bytes<N, L>(warps);
+    auto kern = mi_inverse_kernel<N, L, MODE>;
+    static size_t smem_set = 0;                     // largest dynamic size opted in so far
     if (smem > 48 * 1024 && smem > smem_set) {
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         smem_set = smem;
     }
-    const long long groups = (batch + G::M - 1) / G::M;
-    const long long need = (groups + warps - 1) / warps;
+
+    // how tiles move: tensor copies (n = 32), 1-D bulk copies (16-byte aligned
+    // tiles), or plain loads
+    CUtensorMap map;
+    std::memset(&map, 0, sizeof(map));
+    int copy_mode = kCopyPlain;
+    const bool aligned16 = (reinterpret_cast<uintptr_t>(a) & 15u) == 0;
+    if (aligned16) {
+        if (N == 32) {
+            if (batch <= 0x7fffffffLL && make_tensor_map(&map, a, N, batch, tm)) copy_mode = kCopyTensor;
+        } else if (((long long)tm * N * N) % 4 == 0) {
+            copy_mode = kCopyBulk;
+        }
+    }
+
+    const long long tiles = (batch + tm - 1) / tm;
     if (grid <= 0) {
         int per_sm = 0;
         cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, tpb, smem);
         if (e != cudaSuccess) return e;
         if (per_sm < 1) per_sm = 1;
-        long long cap = (long long)per_sm * device_sm_count();
-        grid = (int)(need < cap ? need : cap);
+        const long long cap = (long long)per_sm * device_sm_count();
+        grid = (int)(tiles < cap ? tiles : cap);
     }
     if (grid < 1) grid = 1;
-    kern<<<grid, tpb, smem, stream>>>(a, perm, info, batch);
+    kern<<<grid, tpb, smem, stream>>>(a, perm, info, batch, copy_mode, map);
     return cudaGetLastError();
 }
 
@@ -51,9 +87,9 @@ extern const launch_fn kTablePartial[33];
 
 }  // namespace mi
 
-#define MI_TABLE(NAME, MODE)                                                                      \
-    const launch_fn NAME[33] = {                                                                  \
-        nullptr,                launch<1, MODE>,  launch<2, MODE>,  launch<3, MODE>,  launch<4, MODE>,  \
+#define MI_TABLE(NAME, MODE)                                                                          \
+    const launch_fn NAME[33] = {                                                                      \
+        nullptr,          launch<1, MODE>,  launch<2, MODE>,  launch<3, MODE>,  launch<4, MODE>,  \
         launch<5, MODE>,  launch<6, MODE>,  launch<7, MODE>,  launch<8, MODE>,  launch<9, MODE>,  \
         launch<10, MODE>, launch<11, MODE>, launch<12, MODE>, launch<13, MODE>, launch<14, MODE>, \
         launch<15, MODE>, launch<16, MODE>, launch<17, MODE>, launch<18, MODE>, launch<19, MODE>, \
