@@ -49,7 +49,7 @@ static void geom_of(int& lanes, int& mpw, int& smem_warp) {
     lanes = L;
     mpw = Geom<N, L>::M;
     // two staged tiles plus the per-matrix scratch, per warp
-    smem_warp = (int)(smem_bytes<N, L>(1) - 1024 - 16);
+    smem_warp = (int)(smem_bytes<N, L, kModeReference>(1) - 1024);
 }
 
 static bool query(int n, int& lanes, int& mpw, int& smem_warp) {

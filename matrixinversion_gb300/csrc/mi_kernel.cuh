@@ -75,7 +75,7 @@ __host__ __device__ constexpr int pow2_at_least(int n) { return n <= 4 ? 4 : (n 
 // Lanes per matrix used by default: two matrices per warp for n > 8 keeps
 // 8 x 8 (n = 32) register blocks, i.e. 16 broadcast values per 64 FMAs.
 __host__ __device__ constexpr int default_lanes(int n, int mode) {
-    return mode == kModePartial ? pow2_at_least(n) : (n > 8 ? 16 : (n > 4 ? 8 : 4));
+    return mode == kModePartial ? pow2_at_least(n) : (n > 16 ? 16 : (n > 4 ? 8 : 4));
 }
 
 // ---------------------------------------------------------------------------
@@ -399,7 +399,7 @@ __device__ __forceinline__ void gj_step(float (&a)[G::R][G::C], float (&ps)[G::R
     const int kr = k % G::RG, kri = k / G::RG;   // pivot-row owner group, register row
     const int kc = k / C, kci = k % C;           // column owner group, register column
     // column k for my rows from lane (rg, kc); row k for my columns from lane
-    // (kr, cg); the pivot from lane (kr, kc) -- straight out of the owners'
+    // (kr, cg); 1/pivot from lane (kr, kc) -- straight out of the owners'
     // registers, no shared-memory round trip
     const int src_c = gb + kc * G::RG + rg;
     const int src_w = gb + cg * G::RG + kr;
@@ -543,237 +543,336 @@ __device__ __forceinline__ void gj_step_partial(float (&a)[G::R][G::C], float (&
 }
 
 // ---------------------------------------------------------------------------
-// One warp: invert its M matrices (stage st0 = first matrix of the warp).
+// Per-warp pipeline.  Each warp owns one shared-memory slot for its M input
+// matrices, a small row buffer for results and its own mbarrier:
+//   wait for group g in the slot -> pivot replay + register block load ->
+//   issue the copy of group g + (warps in grid) into the same slot (it lands
+//   while this warp eliminates) -> n elimination steps in registers ->
+//   results out through the row buffer with coalesced 16-byte stores.
+// No CTA-wide barriers; occupancy is set by registers, not by staging memory.
 // ---------------------------------------------------------------------------
+template <int N, int L, int MODE>
+struct KGeom {
+    using G = Geom<N, L>;
+    static constexpr int H = (G::RG >= 8) ? 1 : 8 / G::RG;      // register rows per output round
+    static constexpr int ORows = G::RG * H;                      // matrix rows per output round
+    static constexpr int Rounds = (G::R + H - 1) / H;
+    // Output rows leave in rounds of ORows rows per matrix, either as tensor
+    // stores from two alternating buffers in the stage layout (OBR x N per
+    // matrix, dense or 128-byte swizzled) or, for odd n / unaligned pointers,
+    // through one buffer with a padded pitch SB and 16-byte or scalar stores.
+    static constexpr int OBR = ORows < N ? ORows : N;
+    static constexpr int SB = (N % 4 == 0) ? (N <= 8 ? 8 : 40) : (N | 1);
+    static constexpr int kSlot = G::M * G::kMat;
+    static constexpr int kOutT = G::M * OBR * N;                  // one tensor-store buffer
+    static constexpr int kOutS = G::M * ORows * SB;
+    static constexpr int kOut = (2 * kOutT > kOutS) ? 2 * kOutT : kOutS;
+    static constexpr int kScr = (MODE == kModePartial) ? G::kScratch : 64;   // partial needs the exchange buffers
+    static constexpr int kScrTotal = G::M * kScr;
+    static constexpr int r4(int x) { return (x + 3) & ~3; }
+    // per-warp region (floats): slot | output rows | scratch | mbarrier; the
+    // output buffers start on a 128-byte boundary (1 KB for n = 32, where one
+    // buffer is a multiple of 1 KB)
+    static constexpr int oOut = (N == 32) ? ((kSlot + 255) & ~255) : ((kSlot + 31) & ~31);
+    static constexpr int oScr = oOut + r4(kOut);
+    static constexpr int oBar = oScr + r4(kScrTotal);
+    static constexpr int kWarp = (oBar + 4 + 255) / 256 * 256;   // 1 KB multiple
+};
+
+// Offsets of the small per-matrix scratch: pivot values, then pivot rows.
+template <class G, int MODE>
+struct ScratchOff {
+    static constexpr int oD = (MODE == kModePartial) ? G::oD : 0;
+    static constexpr int oWin = (MODE == kModePartial) ? G::oWin : 32;
+};
+
+__device__ __forceinline__ void cp_async_4(float* dst, const float* src, bool valid) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(smem_addr(dst)), "l"(src),
+                 "r"(valid ? 4 : 0)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
 template <int N, int L, int MODE>
 struct GeomN : Geom<N, L> {
     static constexpr int kN = N;
     static constexpr int LL = L;
+    static constexpr int oD = ScratchOff<Geom<N, L>, MODE>::oD;
+    static constexpr int oWin = ScratchOff<Geom<N, L>, MODE>::oWin;
 };
 
 template <int N, int L, int MODE>
-__device__ __forceinline__ void invert_warp(float* st0, float* scr0, int lane, int32_t* perm_out,
-                                            int32_t* info_out, long long first, long long batch) {
-    using G = Geom<N, L>;
-    constexpr int R = G::R, C = G::C, M = G::M, P = G::P;
+__global__ void __launch_bounds__(256, 2) mi_inverse_kernel(float* __restrict__ A, int32_t* __restrict__ perm_out,
+                                                            int32_t* __restrict__ info_out, long long batch,
+                                                            int copy_mode, int vec_out,
+                                                            const __grid_constant__ CUtensorMap tmap,
+                                                            const __grid_constant__ CUtensorMap tmap_out) {
+    using G = GeomN<N, L, MODE>;
+    using K = KGeom<N, L, MODE>;
+    constexpr int NN = N * N, R = G::R, C = G::C, M = G::M, P = G::P;
+    extern __shared__ unsigned char smem_raw[];
+    const uintptr_t base = (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int W = blockDim.x >> 5;
+    float* slot = reinterpret_cast<float*>(base) + (size_t)warp * K::kWarp;
+    float* outb = slot + K::oOut;
+    float* scr0 = slot + K::oScr;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(slot + K::oBar);
+
     const int mslot = lane / L, s = lane % L;
     const int rg = s % G::RG, cg = s / G::RG;
-    float* st = st0 + mslot * G::kMat;
-    float* scr = scr0 + mslot * G::kScratch;
+    float* st = slot + mslot * G::kMat;
+    float* scr = scr0 + mslot * K::kScr;
     int* win = reinterpret_cast<int*>(scr + G::oWin);
 
-    // ---- pivot order (reference rules): groups of P lanes, P / L rounds
-    if constexpr (MODE == kModeReference || MODE == kModeReferenceSerial) {
-        constexpr int GP = 32 / P;      // groups per warp
-        constexpr int IM = M / GP;      // matrices per group (= P / L)
-        const int g = lane / P, sp = lane % P;
-        if constexpr (MODE == kModeReferenceSerial || (N & (N - 1)) == 0) {
-            const float* stm[IM];
-            int* winm[IM];
-#pragma unroll
-            for (int q = 0; q < IM; q++) {
-                const int mm = q * GP + g;
-                stm[q] = st0 + mm * G::kMat;
-                winm[q] = reinterpret_cast<int*>(scr0 + mm * G::kScratch + G::oWin);
-            }
-            replay_fast_multi<N, P, IM, MODE>(stm, winm, sp, g * P);
-        } else {
-#pragma unroll 1
-            for (int q = 0; q < IM; ++q) {
-                const int mm = q * GP + g;
-                replay_tracked<N, P, MODE>(st0 + mm * G::kMat,
-                                           reinterpret_cast<int*>(scr0 + mm * G::kScratch + G::oWin), sp, g * P);
-            }
-        }
-        __syncwarp();
-    } else if constexpr (MODE == kModeNone) {
-        for (int t = s; t < N; t += L) win[t] = t;
-        __syncwarp();
-    }
-
-    // ---- register block, rows in pivot order
-    float a[R][C];
-#pragma unroll
-    for (int ri = 0; ri < R; ri++) {
-        const int i = rg + G::RG * ri;
-        int src = i;
-        if constexpr (MODE == kModeReference || MODE == kModeReferenceSerial) src = (i < N) ? win[i] : 0;
-        if constexpr (N == 32 && C % 4 == 0) {
-#pragma unroll
-            for (int h = 0; h < C / 4; h++) {
-                const int c0 = cg * C + 4 * h;
-                const float4 v = *reinterpret_cast<const float4*>(st + src * 32 + ((((c0 >> 2) ^ (src & 7))) << 2));
-                a[ri][4 * h] = v.x; a[ri][4 * h + 1] = v.y; a[ri][4 * h + 2] = v.z; a[ri][4 * h + 3] = v.w;
-            }
-            if (i >= N) {
-#pragma unroll
-                for (int ci = 0; ci < C; ci++) a[ri][ci] = 0.0f;
-            }
-        } else {
-#pragma unroll
-            for (int ci = 0; ci < C; ci++) {
-                const int j = cg * C + ci;
-                a[ri][ci] = (i < N && j < N) ? st[stage_off<N>(src, j)] : 0.0f;
-            }
-        }
-    }
-
-    // ---- n elimination steps
-    float ps[R];
-#pragma unroll
-    for (int ri = 0; ri < R; ri++) ps[ri] = 1.0f;
-    if constexpr (MODE == kModePartial) {
-        using GP_ = GeomN<N, L, MODE>;
-        int ra = s;
-#pragma unroll
-        for (int k = 0; k < N; ++k) gj_step_partial<GP_>(a, ps, k, rg, cg, s, mslot * L, scr, ra);
-        if (s < N) win[s] = ra;
-    } else {
-#pragma unroll
-        for (int k = 0; k < N; ++k) gj_step<G>(a, ps, k, rg, cg, mslot * L, scr);
-    }
-
-    // ---- scale each row by its 1/pivot
-#pragma unroll
-    for (int ri = 0; ri < R; ri++) {
-#pragma unroll
-        for (int q = 0; q < C / 2; q++) {
-            const float2 x = __fmul2_rn(make_float2(a[ri][2 * q], a[ri][2 * q + 1]), make_float2(ps[ri], ps[ri]));
-            a[ri][2 * q] = x.x;
-            a[ri][2 * q + 1] = x.y;
+    if (lane == 0) {
+        mbar_init(bar, 1);
+        fence_mbar_init();
+        if (copy_mode == kCopyTensor) {
+            tma_prefetch_map(&tmap);
+            tma_prefetch_map(&tmap_out);
         }
     }
     __syncwarp();
 
-    // ---- A^-1[i][win[j]] = X[i][j]: scatter columns into the stage
-    int dst[C];
-#pragma unroll
-    for (int ci = 0; ci < C; ci++) {
-        const int j = cg * C + ci;
-        dst[ci] = (j < N) ? win[j] : 0;
-    }
-#pragma unroll
-    for (int ri = 0; ri < R; ri++) {
-        const int i = rg + G::RG * ri;
-        if (i < N) {
-#pragma unroll
-            for (int ci = 0; ci < C; ci++)
-                if (cg * C + ci < N) st[stage_off<N>(i, dst[ci])] = a[ri][ci];
-        }
-    }
-
-    // ---- perm and info (info: first step whose pivot was exactly zero)
-    const long long mb = first + mslot;
-    unsigned zmask = 0u;
-#pragma unroll
-    for (int q = 0; q < (N + L - 1) / L; q++) {
-        const int t = s + q * L;
-        const bool z = (t < N) && (scr[G::oD + t] == 0.0f);
-        zmask |= group_ballot<L>(z, mslot * L) << (q * L);
-        if (perm_out != nullptr && t < N && mb < batch) perm_out[mb * N + t] = win[t];
-    }
-    if (info_out != nullptr && s == 0 && mb < batch) info_out[mb] = zmask ? __ffs(zmask) : 0;
-}
-
-// ---------------------------------------------------------------------------
-// The kernel: persistent CTAs walk tiles of W*M matrices, two tiles in flight.
-// ---------------------------------------------------------------------------
-template <int N, int L, int MODE>
-__global__ void __launch_bounds__(256) mi_inverse_kernel(float* __restrict__ A, int32_t* __restrict__ perm_out,
-                                                         int32_t* __restrict__ info_out, long long batch,
-                                                         int copy_mode, const __grid_constant__ CUtensorMap tmap) {
-    using G = Geom<N, L>;
-    constexpr int NN = N * N;
-    extern __shared__ unsigned char smem_raw[];
-    __shared__ int abort_flag;
-    const uintptr_t base = (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023);
-    const int W = blockDim.x >> 5;
-    const int TM = W * G::M;                      // matrices per tile
-    const int tile_floats = TM * G::kMat;
-    float* stage0 = reinterpret_cast<float*>(base);
-    uint64_t* bars = reinterpret_cast<uint64_t*>(stage0 + 2 * tile_floats);
-    float* scratch = reinterpret_cast<float*>(bars + 2);
-
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const long long tiles = (batch + TM - 1) / TM;
-    const long long full_tiles = batch / TM;
-    const uint32_t tile_bytes = (uint32_t)tile_floats * 4u;
-
-    if (tid == 0) {
-        mbar_init(&bars[0], 1);
-        mbar_init(&bars[1], 1);
-        fence_mbar_init();
-        abort_flag = 0;
-        if (copy_mode == kCopyTensor) tma_prefetch_map(&tmap);
-    }
-    __syncthreads();
-
-    auto async_ok = [&](long long t) {
-        return copy_mode == kCopyTensor || (copy_mode == kCopyBulk && t < full_tiles);
+    const long long groups = (batch + M - 1) / M;
+    const long long gstride = (long long)gridDim.x * W;
+    auto is_async = [&](long long g) {
+        return copy_mode == kCopyTensor || (copy_mode == kCopyBulk && (g + 1) * M <= batch);
     };
-    auto issue_load = [&](long long t, int buf) {
-        float* dst = stage0 + buf * tile_floats;
-        mbar_arrive_expect_tx(&bars[buf], tile_bytes);
-        if (copy_mode == kCopyTensor) tma_load_3d(dst, &tmap, 0, 0, (int)(t * TM), &bars[buf]);
-        else bulk_load(dst, A + t * TM * NN, tile_bytes, &bars[buf]);
+    auto issue = [&](long long g) {
+        const long long first = g * M;
+        if (is_async(g)) {
+            if (lane == 0) {
+                mbar_arrive_expect_tx(bar, (uint32_t)(K::kSlot * 4));
+                if (copy_mode == kCopyTensor) tma_load_3d(slot, &tmap, 0, 0, (int)first, bar);
+                else bulk_load(slot, A + first * NN, (uint32_t)(K::kSlot * 4), bar);
+            }
+        } else {
+            for (int e = lane; e < M * NN; e += 32) {
+                const int m = e / NN, rem = e - m * NN;
+                const int r = rem / N, c = rem - r * N;
+                const bool valid = first + m < batch;
+                cp_async_4(slot + m * G::kMat + stage_off<N>(r, c), valid ? A + first * NN + e : A, valid);
+            }
+            cp_async_commit();
+        }
     };
 
-    long long t = blockIdx.x;
-    if (tid == 0 && t < tiles && async_ok(t)) issue_load(t, 0);
-    for (int it = 0; t < tiles; ++it, t += gridDim.x) {
-        const int buf = it & 1;
-        float* stage = stage0 + buf * tile_floats;
-        const long long tn = t + gridDim.x;
-        if (tid == 0 && tn < tiles && async_ok(tn)) {
-            bulk_wait_read_all();     // the store from the other buffer has read it
-            fence_proxy_async();
-            issue_load(tn, buf ^ 1);
-        }
-        const long long first = t * TM;
-        const int count = (int)min((long long)TM, batch - first);
-        if (async_ok(t)) {
-            if (!mbar_wait(&bars[buf], (uint32_t)((it >> 1) & 1), kWaitLimit)) {
+    long long g = (long long)blockIdx.x * W + warp;
+    uint32_t phase = 0;
+    if (g < groups) issue(g);
+    while (g < groups) {
+        const long long first = g * M;
+        if (is_async(g)) {
+            if (!mbar_wait(bar, phase & 1u, kWaitLimit)) {
                 atomicOr(&g_device_error, 1);
-                abort_flag = 1;
+                break;
             }
+            phase++;
         } else {
-            for (int e = tid; e < TM * NN; e += blockDim.x) {
-                const int m = e / NN, rem = e - m * NN;
-                const int r = rem / N, c = rem - r * N;
-                stage[m * G::kMat + stage_off<N>(r, c)] = (m < count) ? A[first * NN + e] : 0.0f;
+            cp_async_wait_all();
+        }
+        __syncwarp();
+
+        // ---- pivot order (reference rules): groups of P lanes
+        if constexpr (MODE == kModeReference || MODE == kModeReferenceSerial) {
+            constexpr int GP = 32 / P;      // replay groups per warp
+            constexpr int IM = M / GP;      // matrices per replay group (= P / L)
+            const int gi = lane / P, sp = lane % P;
+            if constexpr (MODE == kModeReferenceSerial || (N & (N - 1)) == 0) {
+                const float* stm[IM];
+                int* winm[IM];
+#pragma unroll
+                for (int q = 0; q < IM; q++) {
+                    const int mm = q * GP + gi;
+                    stm[q] = slot + mm * G::kMat;
+                    winm[q] = reinterpret_cast<int*>(scr0 + mm * K::kScr + G::oWin);
+                }
+                replay_fast_multi<N, P, IM, MODE>(stm, winm, sp, gi * P);
+            } else {
+#pragma unroll 1
+                for (int q = 0; q < IM; ++q) {
+                    const int mm = q * GP + gi;
+                    replay_tracked<N, P, MODE>(slot + mm * G::kMat,
+                                               reinterpret_cast<int*>(scr0 + mm * K::kScr + G::oWin), sp, gi * P);
+                }
+            }
+        } else if constexpr (MODE == kModeNone) {
+            for (int t = s; t < N; t += L) win[t] = t;
+        }
+        __syncwarp();
+
+        // ---- register block, rows in pivot order
+        float a[R][C];
+#pragma unroll
+        for (int ri = 0; ri < R; ri++) {
+            const int i = rg + G::RG * ri;
+            int src = i;
+            if constexpr (MODE == kModeReference || MODE == kModeReferenceSerial) src = (i < N) ? win[i] : 0;
+            if constexpr (N == 32 && C % 4 == 0) {
+#pragma unroll
+                for (int h = 0; h < C / 4; h++) {
+                    const int c0 = cg * C + 4 * h;
+                    const float4 v =
+                        *reinterpret_cast<const float4*>(st + src * 32 + ((((c0 >> 2) ^ (src & 7))) << 2));
+                    a[ri][4 * h] = v.x; a[ri][4 * h + 1] = v.y; a[ri][4 * h + 2] = v.z; a[ri][4 * h + 3] = v.w;
+                }
+                if (i >= N) {
+#pragma unroll
+                    for (int ci = 0; ci < C; ci++) a[ri][ci] = 0.0f;
+                }
+            } else {
+#pragma unroll
+                for (int ci = 0; ci < C; ci++) {
+                    const int j = cg * C + ci;
+                    a[ri][ci] = (i < N && j < N) ? st[stage_off<N>(src, j)] : 0.0f;
+                }
             }
         }
-        __syncthreads();
-        if (abort_flag) break;
+        __syncwarp();
 
-        invert_warp<N, L, MODE>(stage + warp * G::M * G::kMat, scratch + warp * G::M * G::kScratch, lane, perm_out,
-                                info_out, first + warp * G::M, batch);
+        // ---- the slot is free: bring in this warp's next group now
+        const long long gn = g + gstride;
+        if (gn < groups) {
+            if (lane == 0) fence_proxy_async();
+            issue(gn);
+        }
 
-        fence_proxy_async();
-        __syncthreads();
-        if (async_ok(t)) {
-            if (tid == 0) {
-                if (copy_mode == kCopyTensor) tma_store_3d(&tmap, 0, 0, (int)first, stage);
-                else bulk_store(A + first * NN, stage, tile_bytes);
-                bulk_commit();
-            }
+        // ---- n elimination steps
+        float ps[R];
+#pragma unroll
+        for (int ri = 0; ri < R; ri++) ps[ri] = 1.0f;
+        if constexpr (MODE == kModePartial) {
+            int ra = s;
+#pragma unroll
+            for (int k = 0; k < N; ++k) gj_step_partial<G>(a, ps, k, rg, cg, s, mslot * L, scr, ra);
+            if (s < N) win[s] = ra;
         } else {
-            for (int e = tid; e < count * NN; e += blockDim.x) {
-                const int m = e / NN, rem = e - m * NN;
-                const int r = rem / N, c = rem - r * N;
-                A[first * NN + e] = stage[m * G::kMat + stage_off<N>(r, c)];
+#pragma unroll
+            for (int k = 0; k < N; ++k) gj_step<G>(a, ps, k, rg, cg, mslot * L, scr);
+        }
+
+        // ---- scale each row by its 1/pivot
+#pragma unroll
+        for (int ri = 0; ri < R; ri++) {
+#pragma unroll
+            for (int q = 0; q < C / 2; q++) {
+                const float2 x =
+                    __fmul2_rn(make_float2(a[ri][2 * q], a[ri][2 * q + 1]), make_float2(ps[ri], ps[ri]));
+                a[ri][2 * q] = x.x;
+                a[ri][2 * q + 1] = x.y;
             }
         }
+        __syncwarp();
+
+        // ---- A^-1[i][win[j]] = X[i][j]: rows leave in rounds of ORows through
+        //      the row buffer (columns scattered there), then coalesced stores
+        int dst[C];
+#pragma unroll
+        for (int ci = 0; ci < C; ci++) {
+            const int j = cg * C + ci;
+            dst[ci] = (j < N) ? win[j] : 0;
+        }
+        if (copy_mode == kCopyTensor) {
+#pragma unroll
+            for (int q = 0; q < K::Rounds; q++) {
+                float* obuf = outb + (q & 1) * K::kOutT;
+                float* ob = obuf + mslot * K::OBR * N;
+                if (lane == 0) bulk_wait_read_one();   // this buffer's store from two rounds ago has read it
+                __syncwarp();
+#pragma unroll
+                for (int h = 0; h < K::H; h++) {
+                    const int ri = q * K::H + h;
+                    const int lr = rg + G::RG * h;
+                    if (ri < R && lr < K::OBR) {
+                        const int i = rg + G::RG * ri;
+                        if (i < N) {
+                            float* orow = ob + lr * N;
+                            const int x = (N == 32) ? ((lr & 7) << 2) : 0;
+#pragma unroll
+                            for (int ci = 0; ci < C; ci++)
+                                if (cg * C + ci < N) orow[dst[ci] ^ x] = a[ri][ci];
+                        }
+                    }
+                }
+                fence_proxy_async();
+                __syncwarp();
+                if (lane == 0) {
+                    tma_store_3d(&tmap_out, 0, q * K::ORows, (int)first, obuf);
+                    bulk_commit();
+                }
+            }
+        } else {
+            float* ob = outb + mslot * K::ORows * K::SB;
+#pragma unroll
+            for (int q = 0; q < K::Rounds; q++) {
+#pragma unroll
+                for (int h = 0; h < K::H; h++) {
+                    const int ri = q * K::H + h;
+                    if (ri < R) {
+                        const int i = rg + G::RG * ri;
+                        if (i < N) {
+                            float* orow = ob + (rg + G::RG * h) * K::SB;
+#pragma unroll
+                            for (int ci = 0; ci < C; ci++)
+                                if (cg * C + ci < N) orow[dst[ci]] = a[ri][ci];
+                        }
+                    }
+                }
+                __syncwarp();
+                const int row0 = q * K::ORows;
+                const int rows = (N - row0 < K::ORows) ? (N - row0) : K::ORows;
+                if (rows > 0) {
+                    if (vec_out && N % 4 == 0) {
+                        constexpr int Q = N / 4;               // 16-byte chunks per row
+                        const int per = rows * Q;
+                        for (int e = lane; e < M * per; e += 32) {
+                            const int m = e / per, rem = e - m * per;
+                            const int r = rem / Q, c4 = rem - r * Q;
+                            if (first + m < batch) {
+                                const float4 v =
+                                    *reinterpret_cast<const float4*>(outb + (m * K::ORows + r) * K::SB + 4 * c4);
+                                *reinterpret_cast<float4*>(A + (first + m) * NN + (row0 + r) * N + 4 * c4) = v;
+                            }
+                        }
+                    } else {
+                        const int per = rows * N;
+                        for (int e = lane; e < M * per; e += 32) {
+                            const int m = e / per, rem = e - m * per;
+                            const int r = rem / N, c = rem - r * N;
+                            if (first + m < batch)
+                                A[(first + m) * NN + (row0 + r) * N + c] = outb[(m * K::ORows + r) * K::SB + c];
+                        }
+                    }
+                }
+                __syncwarp();
+            }
+        }
+
+        // ---- perm and info (info: first step whose pivot was exactly zero)
+        const long long mb = first + mslot;
+        unsigned zmask = 0u;
+#pragma unroll
+        for (int q = 0; q < (N + L - 1) / L; q++) {
+            const int t = s + q * L;
+            const bool z = (t < N) && (scr[G::oD + t] == 0.0f);
+            zmask |= group_ballot<L>(z, mslot * L) << (q * L);
+            if (perm_out != nullptr && t < N && mb < batch) perm_out[mb * N + t] = win[t];
+        }
+        if (info_out != nullptr && s == 0 && mb < batch) info_out[mb] = zmask ? __ffs(zmask) : 0;
+        __syncwarp();
+        g = gn;
     }
-    if (tid == 0) bulk_wait_all();
+    if (lane == 0) bulk_wait_all();
 }
 
-// Shared memory bytes for W warps (1 KB of slack for the 1024-byte alignment).
-template <int N, int L>
+// Dynamic shared memory for a block of `warps` warps (1 KB of slack for the
+// 1024-byte alignment the swizzled tensor copies need).
+template <int N, int L, int MODE>
 constexpr size_t smem_bytes(int warps) {
-    using G = Geom<N, L>;
-    return 1024 + (size_t)2 * warps * G::M * G::kMat * sizeof(float) + 16 +
-           (size_t)warps * G::M * G::kScratch * sizeof(float);
+    return 1024 + (size_t)warps * KGeom<N, L, MODE>::kWarp * sizeof(float);
 }
 
 }  // namespace mi

@@ -21,17 +21,18 @@ constexpr int kDefaultThreadsPerBlock = 128;
 int device_sm_count();                                  // cached per device (mi_api.cu)
 PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder();  // driver entry point (mi_api.cu)
 
-// 3-D tensor map over the batch: {column, row, matrix}, box of one tile,
-// 128-byte swizzle (n = 32 rows are exactly 128 bytes).
-inline bool make_tensor_map(CUtensorMap* map, float* a, int n, long long batch, int tile_matrices) {
+// 3-D tensor map over the batch: {column, row, matrix}, box of one warp's
+// group of matrices; the 128-byte swizzle for n = 32 (rows are 128 bytes).
+inline bool make_tensor_map(CUtensorMap* map, float* a, int n, long long batch, int box_rows, int box_matrices) {
     auto encode = tensor_map_encoder();
     if (encode == nullptr) return false;
     const cuuint64_t dims[3] = {(cuuint64_t)n, (cuuint64_t)n, (cuuint64_t)batch};
     const cuuint64_t strides[2] = {(cuuint64_t)n * 4u, (cuuint64_t)n * n * 4u};
-    const cuuint32_t box[3] = {(cuuint32_t)n, (cuuint32_t)n, (cuuint32_t)tile_matrices};
+    const cuuint32_t box[3] = {(cuuint32_t)n, (cuuint32_t)box_rows, (cuuint32_t)box_matrices};
     const cuuint32_t estr[3] = {1u, 1u, 1u};
     const CUresult r = encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, a, dims, strides, box, estr,
-                              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                              CU_TENSOR_MAP_INTERLEAVE_NONE,
+                              n == 32 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_NONE,
                               CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     return r == CUDA_SUCCESS;
 }
@@ -42,8 +43,7 @@ cudaError_t launch(float* a, int32_t* perm, int32_t* info, long long batch, int 
     constexpr int L = default_lanes(N, MODE);
     using G = Geom<N, L>;
     const int warps = tpb / 32;
-    const int tm = warps * G::M;                    // matrices per tile
-    const size_t smem = smem_bytes<N, L>(warps);
+    const size_t smem = smem_bytes<N, L, MODE>(warps);
     auto kern = mi_inverse_kernel<N, L, MODE>;
     static size_t smem_set = 0;                     // largest dynamic size opted in so far
     if (smem > 48 * 1024 && smem > smem_set) {
@@ -52,31 +52,37 @@ cudaError_t launch(float* a, int32_t* perm, int32_t* info, long long batch, int 
         smem_set = smem;
     }
 
-    // how tiles move: tensor copies (n = 32), 1-D bulk copies (16-byte aligned
-    // tiles), or plain loads
-    CUtensorMap map;
+    // how each warp's group of M matrices moves in: tensor copies (rows of a
+    // multiple of 16 bytes), 1-D bulk copies (16-byte aligned groups), or
+    // per-element asynchronous copies; results leave with 16-byte stores when
+    // rows allow
+    CUtensorMap map, map_out;
     std::memset(&map, 0, sizeof(map));
+    std::memset(&map_out, 0, sizeof(map_out));
     int copy_mode = kCopyPlain;
     const bool aligned16 = (reinterpret_cast<uintptr_t>(a) & 15u) == 0;
     if (aligned16) {
-        if (N == 32) {
-            if (batch <= 0x7fffffffLL && make_tensor_map(&map, a, N, batch, tm)) copy_mode = kCopyTensor;
-        } else if (((long long)tm * N * N) % 4 == 0) {
+        if (N % 4 == 0 && batch <= 0x7fffffffLL && make_tensor_map(&map, a, N, batch, N, G::M) &&
+            make_tensor_map(&map_out, a, N, batch, KGeom<N, L, MODE>::OBR, G::M))
+            copy_mode = kCopyTensor;
+        else if (((long long)G::M * N * N) % 4 == 0)
             copy_mode = kCopyBulk;
-        }
     }
+    const int vec_out = (aligned16 && N % 4 == 0) ? 1 : 0;
+    if (N == 32 && copy_mode != kCopyTensor) copy_mode = kCopyPlain;   // the swizzled layout needs the tensor copy
 
-    const long long tiles = (batch + tm - 1) / tm;
+    const long long groups = (batch + G::M - 1) / G::M;
+    const long long need = (groups + warps - 1) / warps;
     if (grid <= 0) {
         int per_sm = 0;
         cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, tpb, smem);
         if (e != cudaSuccess) return e;
         if (per_sm < 1) per_sm = 1;
         const long long cap = (long long)per_sm * device_sm_count();
-        grid = (int)(tiles < cap ? tiles : cap);
+        grid = (int)(need < cap ? need : cap);
     }
     if (grid < 1) grid = 1;
-    kern<<<grid, tpb, smem, stream>>>(a, perm, info, batch, copy_mode, map);
+    kern<<<grid, tpb, smem, stream>>>(a, perm, info, batch, copy_mode, vec_out, map, map_out);
     return cudaGetLastError();
 }
 
