@@ -20,6 +20,8 @@ INCLUDE = os.path.join(ROOT, "include")
 BUILD = os.path.join(PKG, "_build")
 LIBDIR = os.path.join(PKG, "lib")
 LIB = os.path.join(LIBDIR, "libmi_inverse.so")
+CSRC_CMP = os.path.join(PKG, "csrc_compare")
+LIB_CUBLAS = os.path.join(LIBDIR, "libmi_cublas_ref.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I" + INCLUDE, "-I" + CSRC]
@@ -65,7 +67,20 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
         out = subprocess.run(cmd, capture_output=True, text=True)
         if out.returncode != 0:
             raise RuntimeError("link failed:\n" + out.stderr[-4000:])
+    build_comparator()
     return LIB
+
+
+def build_comparator() -> str:
+    """The cuBLAS getrf+getri comparison library (measurement only)."""
+    src = os.path.join(CSRC_CMP, "mi_cublas_ref.cu")
+    if os.path.exists(LIB_CUBLAS) and os.path.getmtime(LIB_CUBLAS) >= os.path.getmtime(src):
+        return LIB_CUBLAS
+    cmd = [nvcc(), *ARCH, "-O2", "-std=c++17", "-Xcompiler", "-fPIC", "-shared", src, "-o", LIB_CUBLAS, "-lcublas"]
+    out = subprocess.run(cmd, capture_output=True, text=True)
+    if out.returncode != 0:
+        raise RuntimeError("cuBLAS comparator build failed:\n" + out.stderr[-4000:])
+    return LIB_CUBLAS
 
 
 if __name__ == "__main__":

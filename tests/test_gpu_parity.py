@@ -213,3 +213,16 @@ def test_full_size_batch_properties(mi_gpu, oracle):
     assert np.array_equal(Xa, Xs)
     del dA, X1, X2
     torch.cuda.empty_cache()
+
+
+def test_cublas_comparator_is_an_inverse(mi_gpu, oracle):
+    import torch
+
+    from matrixinversion_gb300 import cublas_ref
+
+    A = oracle.uniform(71, 300, 16)
+    (C, piv, info), (t1, t2) = cublas_ref.inverse(torch.from_numpy(A).cuda(), timed=True)
+    X64, _, _ = oracle.inverse_f64(A, "partial")
+    assert (info.cpu().numpy() == 0).all() and t1 > 0 and t2 > 0
+    rel = np.abs(C.cpu().numpy() - X64).max((1, 2)) / np.abs(X64).max((1, 2))
+    assert np.median(rel) < 1e-4
