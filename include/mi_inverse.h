@@ -26,10 +26,19 @@
  *                       matrices per block) and :118 (shared memory).
  *   mi_error_string /   the reference's CUDA_CHECK, which prints and calls
  *   mi_last_cuda_error  exit(1) (parallel_pivot/luBatchedInplace.cuh:9).
+ *   mi_inverse_descr_f32  no reference counterpart for mixed sizes in one
+ *                       call; the per-matrix work is the same kernel, and the
+ *                       runtime-n interface follows no_templ/
+ *                       luBatchedInplace.cuh:82-85 (n, batch and threads as
+ *                       runtime values).
+ *   mi_set_launch_config / mi_get_launch_config  the NUMTHREADS table of
+ *                       parallel_pivot/run.py:187-224, per (n, pivot), settable
+ *                       at run time (by the autotuner).
  */
 #ifndef MI_INVERSE_H
 #define MI_INVERSE_H
 
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -79,6 +88,28 @@ int mi_inverse_cfg_f32(float* d_a, int32_t* d_perm, int32_t* d_info, int64_t bat
  */
 int mi_query_config(int n, int* lanes_per_matrix, int* matrices_per_warp, int* smem_bytes_per_warp,
                     int* default_threads_per_block);
+
+/*
+ * Mixed sizes in one call.  Matrix i is n_i x n_i (1..32), row-major at
+ * d_packed + d_offsets[i] (floats), pivot mode d_flags[i] (MI_PIVOT_*),
+ * inverted in place.  d_perm (nullable) int32[count][32]: pivots of matrix i
+ * at d_perm[i * 32 ..]; d_info (nullable) int32[count]: as mi_inverse_f32,
+ * or -1 for a malformed descriptor (n or flag out of range; not processed).
+ * n_mask: bit n-1 set if size n may occur (0 = all sizes); mode_mask: bit m
+ * set if pivot mode m may occur (0 = all) -- buckets outside the masks are
+ * not launched.  d_workspace: caller-owned device scratch of at least
+ * mi_descr_workspace_bytes(count) bytes, 256-byte aligned.  The call issues
+ * only stream-ordered work (no host synchronisation), so it can be captured
+ * into a CUDA graph.
+ */
+int mi_inverse_descr_f32(float* d_packed, const int64_t* d_offsets, const int32_t* d_n, const int32_t* d_flags,
+                         int32_t* d_perm, int32_t* d_info, int64_t count, uint32_t n_mask, uint32_t mode_mask,
+                         void* d_workspace, size_t workspace_bytes, void* stream);
+size_t mi_descr_workspace_bytes(int64_t count);
+
+/* Threads per block used for size n and pivot mode (0 = built-in default). */
+int mi_set_launch_config(int n, int pivot, int threads_per_block);
+int mi_get_launch_config(int n, int pivot, int* threads_per_block);
 
 const char* mi_error_string(int status);
 /* Text of the last CUDA error seen by this thread ("" if none). */

@@ -55,6 +55,15 @@ def load(path: str | None = None):
     L.mi_last_cuda_error.restype = ctypes.c_char_p
     L.mi_abi_version.argtypes = []
     L.mi_abi_version.restype = i32
+    L.mi_inverse_descr_f32.argtypes = [vp, vp, vp, vp, vp, vp, i64, ctypes.c_uint32, ctypes.c_uint32, vp,
+                                       ctypes.c_size_t, vp]
+    L.mi_inverse_descr_f32.restype = i32
+    L.mi_descr_workspace_bytes.argtypes = [i64]
+    L.mi_descr_workspace_bytes.restype = ctypes.c_size_t
+    L.mi_set_launch_config.argtypes = [i32, i32, i32]
+    L.mi_set_launch_config.restype = i32
+    L.mi_get_launch_config.argtypes = [i32, i32, ip]
+    L.mi_get_launch_config.restype = i32
     _lib = L
     return L
 
@@ -77,4 +86,8 @@ def exported_symbols() -> list[str]:
         "mi_error_string",
         "mi_last_cuda_error",
         "mi_abi_version",
+        "mi_inverse_descr_f32",
+        "mi_descr_workspace_bytes",
+        "mi_set_launch_config",
+        "mi_get_launch_config",
     ]

@@ -18,6 +18,16 @@ static int cuda_fail(cudaError_t e, const char* what) {
     return MI_ERR_CUDA;
 }
 
+int set_cuda_error(cudaError_t e, const char* what) { return cuda_fail(e, what); }
+
+// Threads per block per (n, pivot mode): 0 = the default; set by the autotuner.
+static int g_tuned[33][4] = {};
+
+int tuned_threads(int n, int mode) {
+    const int t = (n >= 1 && n <= 32 && mode >= 0 && mode < 4) ? g_tuned[n][mode] : 0;
+    return t > 0 ? t : kDefaultThreadsPerBlock;
+}
+
 int device_sm_count() {
     static int cached[64] = {0};
     int dev = 0;
@@ -108,7 +118,7 @@ int mi_inverse_cfg_f32(float* d_a, int32_t* d_perm, int32_t* d_info, int64_t bat
     if (batch == 0) return MI_OK;
     if (d_a == nullptr) return MI_ERR_NULL_POINTER;
     if ((reinterpret_cast<uintptr_t>(d_a) & 3u) != 0) return MI_ERR_MISALIGNED;
-    int tpb = threads_per_block == 0 ? mi::kDefaultThreadsPerBlock : threads_per_block;
+    int tpb = threads_per_block == 0 ? mi::tuned_threads(n, pivot) : threads_per_block;
     tpb = (tpb + 31) / 32 * 32;
     if (tpb > mi::kMaxThreadsPerBlock) tpb = mi::kMaxThreadsPerBlock;
     cudaError_t e = table[n](d_a, d_perm, d_info, (long long)batch, tpb, grid_blocks,
@@ -120,6 +130,20 @@ int mi_inverse_cfg_f32(float* d_a, int32_t* d_perm, int32_t* d_info, int64_t bat
 int mi_inverse_f32(float* d_a, int32_t* d_perm, int32_t* d_info, int64_t batch, int n, int pivot,
                    void* stream) {
     return mi_inverse_cfg_f32(d_a, d_perm, d_info, batch, n, pivot, 0, 0, stream);
+}
+
+int mi_set_launch_config(int n, int pivot, int threads_per_block) {
+    if (n < 1 || n > 32 || pivot < 0 || pivot > 3 || threads_per_block < 0 || threads_per_block > 256 ||
+        threads_per_block % 32 != 0)
+        return MI_ERR_INVALID_VALUE;
+    mi::g_tuned[n][pivot] = threads_per_block;
+    return MI_OK;
+}
+
+int mi_get_launch_config(int n, int pivot, int* threads_per_block) {
+    if (n < 1 || n > 32 || pivot < 0 || pivot > 3) return MI_ERR_INVALID_VALUE;
+    if (threads_per_block) *threads_per_block = mi::tuned_threads(n, pivot);
+    return MI_OK;
 }
 
 }  // extern "C"

@@ -1,0 +1,121 @@
+// mi_descr.cu -- mixed sizes in one call: an (offset, n, pivot flag)
+// descriptor table is bucketed by (n, flag) on the GPU (count, scan, scatter
+// into caller-provided workspace), then one persistent indexed launch per
+// bucket walks that bucket's matrices.  Nothing waits on the host between
+// the steps, so the whole call can be captured into one CUDA graph.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "mi_inverse.h"
+#include "mi_launch.cuh"
+
+namespace mi {
+
+constexpr int kBuckets = 32 * 4;                 // (n - 1) * 4 + mode
+constexpr size_t kOffCounts = 0;                 // unsigned long long[128]
+constexpr size_t kOffCursors = 1024;             // unsigned long long[128]
+constexpr size_t kOffRanges = 2048;              // long long[128][2]: start, count
+constexpr size_t kOffList = 4096;                // int32[count]
+
+__global__ void descr_count(const int32_t* __restrict__ ns, const int32_t* __restrict__ flags, long long count,
+                            unsigned long long* __restrict__ counts, int32_t* __restrict__ info) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < count;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int n = ns[i], f = flags[i];
+        if (n >= 1 && n <= 32 && f >= 0 && f <= 3) atomicAdd(&counts[(n - 1) * 4 + f], 1ull);
+        else if (info != nullptr) info[i] = -1;   // malformed descriptor: reported, not processed
+    }
+}
+
+__global__ void descr_scan(const unsigned long long* __restrict__ counts, unsigned long long* __restrict__ cursors,
+                           long long* __restrict__ ranges) {
+    __shared__ unsigned long long c[kBuckets];
+    const int t = threadIdx.x;
+    c[t] = counts[t];
+    __syncthreads();
+    if (t == 0) {
+        unsigned long long run = 0;
+        for (int b = 0; b < kBuckets; b++) {
+            const unsigned long long v = c[b];
+            c[b] = run;
+            run += v;
+        }
+    }
+    __syncthreads();
+    cursors[t] = c[t];
+    ranges[2 * t] = (long long)c[t];
+    ranges[2 * t + 1] = (long long)counts[t];
+}
+
+__global__ void descr_scatter(const int32_t* __restrict__ ns, const int32_t* __restrict__ flags, long long count,
+                              unsigned long long* __restrict__ cursors, int32_t* __restrict__ list) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < count;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int n = ns[i], f = flags[i];
+        if (n >= 1 && n <= 32 && f >= 0 && f <= 3) {
+            const unsigned long long p = atomicAdd(&cursors[(n - 1) * 4 + f], 1ull);
+            list[p] = (int32_t)i;
+        }
+    }
+}
+
+int tuned_threads(int n, int mode);   // mi_api.cu
+int set_cuda_error(cudaError_t e, const char* what);
+
+}  // namespace mi
+
+extern "C" {
+
+size_t mi_descr_workspace_bytes(int64_t count) {
+    if (count < 0) return 0;
+    return (mi::kOffList + 4 * (size_t)count + 255) & ~(size_t)255;
+}
+
+int mi_inverse_descr_f32(float* d_packed, const int64_t* d_offsets, const int32_t* d_n, const int32_t* d_flags,
+                         int32_t* d_perm, int32_t* d_info, int64_t count, uint32_t n_mask, uint32_t mode_mask,
+                         void* d_workspace, size_t workspace_bytes, void* stream) {
+    if (count < 0 || count > 0x7fffffffLL) return MI_ERR_INVALID_VALUE;
+    if (count == 0) return MI_OK;
+    if (d_packed == nullptr || d_offsets == nullptr || d_n == nullptr || d_flags == nullptr || d_workspace == nullptr)
+        return MI_ERR_NULL_POINTER;
+    if ((reinterpret_cast<uintptr_t>(d_packed) & 3u) != 0 || (reinterpret_cast<uintptr_t>(d_workspace) & 255u) != 0)
+        return MI_ERR_MISALIGNED;
+    if (workspace_bytes < mi_descr_workspace_bytes(count)) return MI_ERR_INVALID_VALUE;
+    if (n_mask == 0) n_mask = 0xffffffffu;
+    if (mode_mask == 0) mode_mask = 0xfu;
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    unsigned char* ws = static_cast<unsigned char*>(d_workspace);
+    auto* counts = reinterpret_cast<unsigned long long*>(ws + mi::kOffCounts);
+    auto* cursors = reinterpret_cast<unsigned long long*>(ws + mi::kOffCursors);
+    auto* ranges = reinterpret_cast<long long*>(ws + mi::kOffRanges);
+    auto* list = reinterpret_cast<int32_t*>(ws + mi::kOffList);
+
+    cudaError_t e = cudaMemsetAsync(counts, 0, mi::kBuckets * sizeof(unsigned long long), st);
+    if (e != cudaSuccess) return mi::set_cuda_error(e, "descriptor bucketing");
+    const int sms = mi::device_sm_count();
+    long long blocks = (count + 255) / 256;
+    if (blocks > 4LL * sms) blocks = 4LL * sms;
+    mi::descr_count<<<(unsigned)blocks, 256, 0, st>>>(d_n, d_flags, count, counts, d_info);
+    mi::descr_scan<<<1, mi::kBuckets, 0, st>>>(counts, cursors, ranges);
+    mi::descr_scatter<<<(unsigned)blocks, 256, 0, st>>>(d_n, d_flags, count, cursors, list);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return mi::set_cuda_error(e, "descriptor bucketing");
+
+    const mi::ilaunch_fn* tables[4] = {mi::kITableNone, mi::kITableReference, mi::kITableReferenceSerial,
+                                       mi::kITablePartial};
+    const long long* off64 = reinterpret_cast<const long long*>(d_offsets);
+    for (int n = 1; n <= 32; n++) {
+        if (!((n_mask >> (n - 1)) & 1u)) continue;
+        for (int mode = 0; mode < 4; mode++) {
+            if (!((mode_mask >> mode) & 1u)) continue;
+            const int b = (n - 1) * 4 + mode;
+            e = tables[mode][n](d_packed, off64, list, ranges + 2 * b, d_perm, d_info, mi::tuned_threads(n, mode), 0,
+                                st);
+            if (e != cudaSuccess) return mi::set_cuda_error(e, "descriptor bucket launch");
+        }
+    }
+    return MI_OK;
+}
+
+}  // extern "C"

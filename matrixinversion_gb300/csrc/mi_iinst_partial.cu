@@ -1,0 +1,7 @@
+// Instantiations of the indexed (descriptor bucket) inverse kernel for
+// n = 1..32, pivot mode partial.
+#include "mi_launch.cuh"
+
+namespace mi {
+MI_ITABLE(kITablePartial, kModePartial);
+}  // namespace mi

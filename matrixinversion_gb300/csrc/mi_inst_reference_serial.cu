@@ -1,4 +1,5 @@
-// Instantiations of the inverse kernel for n = 1..32, pivot mode reference_serial.
+// Instantiations of the contiguous-batch inverse kernel for n = 1..32,
+// pivot mode reference_serial.
 #include "mi_launch.cuh"
 
 namespace mi {

@@ -111,9 +111,9 @@ struct Geom {
 // Stage layout of one matrix: row-major, with the TMA 128-byte swizzle
 // (16-byte chunk index XOR row & 7) for n = 32 so that both row-wise and
 // column-block accesses from a warp are free of bank conflicts.
-template <int N>
+template <int N, bool SW = (N == 32)>
 __device__ __forceinline__ int stage_off(int r, int c) {
-    if constexpr (N == 32) return r * 32 + ((((c >> 2) ^ (r & 7)) << 2) | (c & 3));
+    if constexpr (SW) return r * 32 + ((((c >> 2) ^ (r & 7)) << 2) | (c & 3));
     else return r * N + c;
 }
 
@@ -265,7 +265,7 @@ __device__ __forceinline__ void row_update(float (&a)[C], float m, const float (
 // Exact rule for one step k, from scratch: positions after steps 0..k-1 are
 // rebuilt from win[], then the reference's tree (or serial scan) runs on the
 // raw entries with its own tie order and dropped slots.  Returns the row.
-template <int N, int P, int MODE>
+template <int N, int P, int MODE, bool SW = (N == 32)>
 __device__ __noinline__ int exact_pivot(const float* st, const int* win, int k, int s, int gbase) {
     __syncwarp();
     int pos = (s < N) ? s : 0x7fff;
@@ -275,7 +275,7 @@ __device__ __noinline__ int exact_pivot(const float* st, const int* win, int k, 
         if (s == wj) pos = j;
         else if (pos == j) pos = pw;
     }
-    const unsigned kraw = (s < N) ? pivot_key(st[stage_off<N>(s, k)]) : 0u;
+    const unsigned kraw = (s < N) ? pivot_key(st[stage_off<N, SW>(s, k)]) : 0u;
     const int dl = __ffs(group_ballot<P>(pos == k, gbase)) - 1;
     const unsigned kd = __shfl_sync(kFull, kraw, gbase + dl);
     const int slot = pos - k - 1;
@@ -292,16 +292,16 @@ __device__ __noinline__ int exact_pivot(const float* st, const int* win, int k, 
 }
 
 // Keys of row r, columns k0..k0+3 (0 past the matrix).
-template <int N>
+template <int N, bool SW = (N == 32)>
 __device__ __forceinline__ void load_keys4(const float* st, int r, int k0, unsigned (&kv)[4]) {
     if (r >= N) {
 #pragma unroll
         for (int t = 0; t < 4; t++) kv[t] = 0u;
         return;
     }
-    if constexpr (N == 32 || N % 4 == 0) {
-        const float4 v = *reinterpret_cast<const float4*>(st + ((N == 32) ? (r * 32 + ((((k0 >> 2) ^ (r & 7))) << 2))
-                                                                        : (r * N + k0)));
+    if constexpr (N % 4 == 0) {
+        const float4 v = *reinterpret_cast<const float4*>(st + (SW ? (r * 32 + ((((k0 >> 2) ^ (r & 7))) << 2))
+                                                                  : (r * N + k0)));
         kv[0] = fast_key(v.x); kv[1] = fast_key(v.y); kv[2] = fast_key(v.z); kv[3] = fast_key(v.w);
     } else {
 #pragma unroll
@@ -312,7 +312,7 @@ __device__ __forceinline__ void load_keys4(const float* st, int r, int k0, unsig
 // The fast replay for IM matrices at once, one independent chain each, so
 // the reduction latencies of the chains overlap; keys are read from the
 // stage four columns at a time (a compact, rolled loop).
-template <int N, int P, int IM, int MODE>
+template <int N, int P, int IM, int MODE, bool SW = (N == 32)>
 __device__ __forceinline__ void replay_fast_multi(const float* const (&st)[IM], int* const (&win)[IM], int s,
                                                   int gbase) {
     bool placed[IM];
@@ -322,7 +322,7 @@ __device__ __forceinline__ void replay_fast_multi(const float* const (&st)[IM], 
     for (int k0 = 0; k0 < N; k0 += 4) {
         unsigned kv[IM][4];
 #pragma unroll
-        for (int m = 0; m < IM; m++) load_keys4<N>(st[m], s, k0, kv[m]);
+        for (int m = 0; m < IM; m++) load_keys4<N, SW>(st[m], s, k0, kv[m]);
 #pragma unroll
         for (int t = 0; t < 4; t++) {
             const int k = k0 + t;
@@ -339,7 +339,7 @@ __device__ __forceinline__ void replay_fast_multi(const float* const (&st)[IM], 
                 int w[IM];
                 if (__any_sync(kFull, rare)) {
 #pragma unroll
-                    for (int m = 0; m < IM; m++) w[m] = exact_pivot<N, P, MODE>(st[m], win[m], k, s, gbase);
+                    for (int m = 0; m < IM; m++) w[m] = exact_pivot<N, P, MODE, SW>(st[m], win[m], k, s, gbase);
                 } else {
 #pragma unroll
                     for (int m = 0; m < IM; m++) w[m] = __ffs(tb[m]) - 1;
@@ -356,12 +356,12 @@ __device__ __forceinline__ void replay_fast_multi(const float* const (&st)[IM], 
 
 // Non-power-of-two n under the reference rule: some tree slots are dropped,
 // so positions are tracked every step (lane = row).
-template <int N, int P, int MODE>
+template <int N, int P, int MODE, bool SW = (N == 32)>
 __device__ __forceinline__ void replay_tracked(const float* st, int* win, int s, int gbase) {
     constexpr unsigned kSurv = survive_mask(N);
     unsigned key[N];
 #pragma unroll
-    for (int k = 0; k < N; k++) key[k] = (s < N) ? pivot_key(st[stage_off<N>(s, k)]) : 0u;
+    for (int k = 0; k < N; k++) key[k] = (s < N) ? pivot_key(st[stage_off<N, SW>(s, k)]) : 0u;
     int pos = (s < N) ? s : 0x7fff;
 #pragma unroll
     for (int k = 0; k < N; ++k) {
@@ -602,6 +602,265 @@ struct GeomN : Geom<N, L> {
     static constexpr int oWin = ScratchOff<Geom<N, L>, MODE>::oWin;
 };
 
+// ---- phase A: pivot order (reference rules) and the register block, rows in
+// pivot order, from the warp's slot (stage layout SW).
+template <int N, int L, int MODE, bool SW>
+__device__ __forceinline__ void phase_load(float (&a)[GeomN<N, L, MODE>::R][GeomN<N, L, MODE>::C], const float* slot,
+                                           float* scr0, int lane) {
+    using G = GeomN<N, L, MODE>;
+    using K = KGeom<N, L, MODE>;
+    constexpr int R = G::R, C = G::C, M = G::M, P = G::P;
+    const int mslot = lane / L, s = lane % L;
+    const int rg = s % G::RG, cg = s / G::RG;
+    const float* st = slot + mslot * G::kMat;
+    int* win = reinterpret_cast<int*>(scr0 + mslot * K::kScr + G::oWin);
+    if constexpr (MODE == kModeReference || MODE == kModeReferenceSerial) {
+        constexpr int GP = 32 / P;      // replay groups per warp
+        constexpr int IM = M / GP;      // matrices per replay group (= P / L)
+        const int gi = lane / P, sp = lane % P;
+        if constexpr (MODE == kModeReferenceSerial || (N & (N - 1)) == 0) {
+            const float* stm[IM];
+            int* winm[IM];
+#pragma unroll
+            for (int q = 0; q < IM; q++) {
+                const int mm = q * GP + gi;
+                stm[q] = slot + mm * G::kMat;
+                winm[q] = reinterpret_cast<int*>(scr0 + mm * K::kScr + G::oWin);
+            }
+            replay_fast_multi<N, P, IM, MODE, SW>(stm, winm, sp, gi * P);
+        } else {
+#pragma unroll 1
+            for (int q = 0; q < IM; ++q) {
+                const int mm = q * GP + gi;
+                replay_tracked<N, P, MODE, SW>(slot + mm * G::kMat,
+                                               reinterpret_cast<int*>(scr0 + mm * K::kScr + G::oWin), sp, gi * P);
+            }
+        }
+    } else if constexpr (MODE == kModeNone) {
+        for (int t = s; t < N; t += L) win[t] = t;
+    }
+    __syncwarp();
+#pragma unroll
+    for (int ri = 0; ri < R; ri++) {
+        const int i = rg + G::RG * ri;
+        int src = i;
+        if constexpr (MODE == kModeReference || MODE == kModeReferenceSerial) src = (i < N) ? win[i] : 0;
+        if constexpr (N % 4 == 0 && C % 4 == 0) {
+#pragma unroll
+            for (int h = 0; h < C / 4; h++) {
+                const int c0 = cg * C + 4 * h;
+                float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (c0 < N) v = *reinterpret_cast<const float4*>(st + stage_off<N, SW>(src, c0));
+                a[ri][4 * h] = v.x; a[ri][4 * h + 1] = v.y; a[ri][4 * h + 2] = v.z; a[ri][4 * h + 3] = v.w;
+            }
+            if (i >= N) {
+#pragma unroll
+                for (int ci = 0; ci < C; ci++) a[ri][ci] = 0.0f;
+            }
+        } else {
+#pragma unroll
+            for (int ci = 0; ci < C; ci++) {
+                const int j = cg * C + ci;
+                a[ri][ci] = (i < N && j < N) ? st[stage_off<N, SW>(src, j)] : 0.0f;
+            }
+        }
+    }
+    __syncwarp();
+}
+
+// ---- phase B: n elimination steps and the final row scaling.
+template <int N, int L, int MODE>
+__device__ __forceinline__ void phase_eliminate(float (&a)[GeomN<N, L, MODE>::R][GeomN<N, L, MODE>::C], float* scr0,
+                                                int lane) {
+    using G = GeomN<N, L, MODE>;
+    using K = KGeom<N, L, MODE>;
+    constexpr int R = G::R, C = G::C;
+    const int mslot = lane / L, s = lane % L;
+    const int rg = s % G::RG, cg = s / G::RG;
+    float* scr = scr0 + mslot * K::kScr;
+    float ps[R];
+#pragma unroll
+    for (int ri = 0; ri < R; ri++) ps[ri] = 1.0f;
+    if constexpr (MODE == kModePartial) {
+        int ra = s;
+#pragma unroll
+        for (int k = 0; k < N; ++k) gj_step_partial<G>(a, ps, k, rg, cg, s, mslot * L, scr, ra);
+        if (s < N) reinterpret_cast<int*>(scr + G::oWin)[s] = ra;
+    } else {
+#pragma unroll
+        for (int k = 0; k < N; ++k) gj_step<G>(a, ps, k, rg, cg, mslot * L, scr);
+    }
+#pragma unroll
+    for (int ri = 0; ri < R; ri++) {
+#pragma unroll
+        for (int q = 0; q < C / 2; q++) {
+            const float2 x = __fmul2_rn(make_float2(a[ri][2 * q], a[ri][2 * q + 1]), make_float2(ps[ri], ps[ri]));
+            a[ri][2 * q] = x.x;
+            a[ri][2 * q + 1] = x.y;
+        }
+    }
+    __syncwarp();
+}
+
+// Destination column of each register column: A^-1[i][win[j]] = X[i][j].
+template <int N, int L, int MODE>
+__device__ __forceinline__ void dest_columns(int (&dst)[GeomN<N, L, MODE>::C], const float* scr0, int lane) {
+    using G = GeomN<N, L, MODE>;
+    using K = KGeom<N, L, MODE>;
+    const int mslot = lane / L, s = lane % L;
+    const int cg = s / G::RG;
+    const int* win = reinterpret_cast<const int*>(scr0 + mslot * K::kScr + G::oWin);
+#pragma unroll
+    for (int ci = 0; ci < G::C; ci++) {
+        const int j = cg * G::C + ci;
+        dst[ci] = (j < N) ? win[j] : 0;
+    }
+}
+
+// ---- phase C1: rows leave in rounds through two alternating buffers in the
+// stage layout, each round one tensor store of ORows rows of the M matrices.
+template <int N, int L, int MODE>
+__device__ __forceinline__ void phase_store_tensor(const float (&a)[GeomN<N, L, MODE>::R][GeomN<N, L, MODE>::C],
+                                                   float* outb, const float* scr0, int lane, const CUtensorMap* tmap_out,
+                                                   long long first) {
+    using G = GeomN<N, L, MODE>;
+    using K = KGeom<N, L, MODE>;
+    constexpr int R = G::R, C = G::C;
+    const int mslot = lane / L, s = lane % L;
+    const int rg = s % G::RG, cg = s / G::RG;
+    int dst[C];
+    dest_columns<N, L, MODE>(dst, scr0, lane);
+#pragma unroll
+    for (int q = 0; q < K::Rounds; q++) {
+        float* obuf = outb + (q & 1) * K::kOutT;
+        float* ob = obuf + mslot * K::OBR * N;
+        if (lane == 0) bulk_wait_read_one();   // this buffer's store from two rounds ago has read it
+        __syncwarp();
+#pragma unroll
+        for (int h = 0; h < K::H; h++) {
+            const int ri = q * K::H + h;
+            const int lr = rg + G::RG * h;
+            if (ri < R && lr < K::OBR) {
+                const int i = rg + G::RG * ri;
+                if (i < N) {
+                    float* orow = ob + lr * N;
+                    const int x = (N == 32) ? ((lr & 7) << 2) : 0;
+#pragma unroll
+                    for (int ci = 0; ci < C; ci++)
+                        if (cg * C + ci < N) orow[dst[ci] ^ x] = a[ri][ci];
+                }
+            }
+        }
+        fence_proxy_async();
+        __syncwarp();
+        if (lane == 0) {
+            tma_store_3d(tmap_out, 0, q * K::ORows, (int)first, obuf);
+            bulk_commit();
+        }
+    }
+}
+
+// ---- phase C2: rows leave through one padded buffer with plain stores to the
+// M matrices at gout[m] (nullptr = no matrix); 16-byte stores when `vec`.
+template <int N, int L, int MODE>
+__device__ __forceinline__ void phase_store_rows(const float (&a)[GeomN<N, L, MODE>::R][GeomN<N, L, MODE>::C],
+                                                 float* outb, const float* scr0, int lane,
+                                                 float* const (&gout)[GeomN<N, L, MODE>::M], bool vec) {
+    using G = GeomN<N, L, MODE>;
+    using K = KGeom<N, L, MODE>;
+    constexpr int R = G::R, C = G::C, M = G::M;
+    const int mslot = lane / L, s = lane % L;
+    const int rg = s % G::RG, cg = s / G::RG;
+    int dst[C];
+    dest_columns<N, L, MODE>(dst, scr0, lane);
+    float* ob = outb + mslot * K::ORows * K::SB;
+#pragma unroll
+    for (int q = 0; q < K::Rounds; q++) {
+#pragma unroll
+        for (int h = 0; h < K::H; h++) {
+            const int ri = q * K::H + h;
+            if (ri < R) {
+                const int i = rg + G::RG * ri;
+                if (i < N) {
+                    float* orow = ob + (rg + G::RG * h) * K::SB;
+#pragma unroll
+                    for (int ci = 0; ci < C; ci++)
+                        if (cg * C + ci < N) orow[dst[ci]] = a[ri][ci];
+                }
+            }
+        }
+        __syncwarp();
+        const int row0 = q * K::ORows;
+        const int rows = (N - row0 < K::ORows) ? (N - row0) : K::ORows;
+        if (rows > 0) {
+            if (N % 4 == 0 && vec) {
+                constexpr int Q = N / 4;               // 16-byte chunks per row
+                const int per = rows * Q;
+                for (int e = lane; e < M * per; e += 32) {
+                    const int m = e / per, rem = e - m * per;
+                    const int r = rem / Q, c4 = rem - r * Q;
+                    if (gout[m] != nullptr) {
+                        const float4 v = *reinterpret_cast<const float4*>(outb + (m * K::ORows + r) * K::SB + 4 * c4);
+                        *reinterpret_cast<float4*>(gout[m] + (row0 + r) * N + 4 * c4) = v;
+                    }
+                }
+            } else {
+                const int per = rows * N;
+                for (int e = lane; e < M * per; e += 32) {
+                    const int m = e / per, rem = e - m * per;
+                    const int r = rem / N, c = rem - r * N;
+                    if (gout[m] != nullptr) gout[m][(row0 + r) * N + c] = outb[(m * K::ORows + r) * K::SB + c];
+                }
+            }
+        }
+        __syncwarp();
+    }
+}
+
+// ---- phase D: pivots and info of this lane's matrix at output index `idx`
+// (negative: no matrix); perm rows have pitch `perm_pitch`.
+template <int N, int L, int MODE>
+__device__ __forceinline__ void phase_perm_info(const float* scr0, int lane, long long idx, int32_t* perm_out,
+                                                int perm_pitch, int32_t* info_out) {
+    using G = GeomN<N, L, MODE>;
+    using K = KGeom<N, L, MODE>;
+    const int mslot = lane / L, s = lane % L;
+    const float* scr = scr0 + mslot * K::kScr;
+    const int* win = reinterpret_cast<const int*>(scr + G::oWin);
+    unsigned zmask = 0u;
+#pragma unroll
+    for (int q = 0; q < (N + L - 1) / L; q++) {
+        const int t = s + q * L;
+        const bool z = (t < N) && (scr[G::oD + t] == 0.0f);
+        zmask |= group_ballot<L>(z, mslot * L) << (q * L);
+        if (perm_out != nullptr && t < N && idx >= 0) perm_out[idx * perm_pitch + t] = win[t];
+    }
+    if (info_out != nullptr && s == 0 && idx >= 0) info_out[idx] = zmask ? __ffs(zmask) : 0;
+    __syncwarp();
+}
+
+// Per-warp shared memory carving.
+template <int N, int L, int MODE>
+struct WarpSmem {
+    float* slot;
+    float* outb;
+    float* scr0;
+    uint64_t* bar;
+    __device__ __forceinline__ WarpSmem(unsigned char* smem_raw, int warp) {
+        using K = KGeom<N, L, MODE>;
+        const uintptr_t base = (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023);
+        slot = reinterpret_cast<float*>(base) + (size_t)warp * K::kWarp;
+        outb = slot + K::oOut;
+        scr0 = slot + K::oScr;
+        bar = reinterpret_cast<uint64_t*>(slot + K::oBar);
+    }
+};
+
+// ---------------------------------------------------------------------------
+// Contiguous batch: matrix b at A + b*n*n.  Persistent warps walk groups of M
+// matrices; one slot per warp, the next group's copy issued right after the
+// block load.
+// ---------------------------------------------------------------------------
 template <int N, int L, int MODE>
 __global__ void __launch_bounds__(256, 2) mi_inverse_kernel(float* __restrict__ A, int32_t* __restrict__ perm_out,
                                                             int32_t* __restrict__ info_out, long long batch,
@@ -610,24 +869,15 @@ __global__ void __launch_bounds__(256, 2) mi_inverse_kernel(float* __restrict__ 
                                                             const __grid_constant__ CUtensorMap tmap_out) {
     using G = GeomN<N, L, MODE>;
     using K = KGeom<N, L, MODE>;
-    constexpr int NN = N * N, R = G::R, C = G::C, M = G::M, P = G::P;
+    constexpr int NN = N * N, R = G::R, C = G::C, M = G::M;
     extern __shared__ unsigned char smem_raw[];
-    const uintptr_t base = (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int W = blockDim.x >> 5;
-    float* slot = reinterpret_cast<float*>(base) + (size_t)warp * K::kWarp;
-    float* outb = slot + K::oOut;
-    float* scr0 = slot + K::oScr;
-    uint64_t* bar = reinterpret_cast<uint64_t*>(slot + K::oBar);
-
-    const int mslot = lane / L, s = lane % L;
-    const int rg = s % G::RG, cg = s / G::RG;
-    float* st = slot + mslot * G::kMat;
-    float* scr = scr0 + mslot * K::kScr;
-    int* win = reinterpret_cast<int*>(scr + G::oWin);
+    const WarpSmem<N, L, MODE> sm(smem_raw, warp);
+    const int mslot = lane / L;
 
     if (lane == 0) {
-        mbar_init(bar, 1);
+        mbar_init(sm.bar, 1);
         fence_mbar_init();
         if (copy_mode == kCopyTensor) {
             tma_prefetch_map(&tmap);
@@ -645,16 +895,16 @@ __global__ void __launch_bounds__(256, 2) mi_inverse_kernel(float* __restrict__ 
         const long long first = g * M;
         if (is_async(g)) {
             if (lane == 0) {
-                mbar_arrive_expect_tx(bar, (uint32_t)(K::kSlot * 4));
-                if (copy_mode == kCopyTensor) tma_load_3d(slot, &tmap, 0, 0, (int)first, bar);
-                else bulk_load(slot, A + first * NN, (uint32_t)(K::kSlot * 4), bar);
+                mbar_arrive_expect_tx(sm.bar, (uint32_t)(K::kSlot * 4));
+                if (copy_mode == kCopyTensor) tma_load_3d(sm.slot, &tmap, 0, 0, (int)first, sm.bar);
+                else bulk_load(sm.slot, A + first * NN, (uint32_t)(K::kSlot * 4), sm.bar);
             }
         } else {
             for (int e = lane; e < M * NN; e += 32) {
                 const int m = e / NN, rem = e - m * NN;
                 const int r = rem / N, c = rem - r * N;
                 const bool valid = first + m < batch;
-                cp_async_4(slot + m * G::kMat + stage_off<N>(r, c), valid ? A + first * NN + e : A, valid);
+                cp_async_4(sm.slot + m * G::kMat + stage_off<N>(r, c), valid ? A + first * NN + e : A, valid);
             }
             cp_async_commit();
         }
@@ -666,7 +916,7 @@ __global__ void __launch_bounds__(256, 2) mi_inverse_kernel(float* __restrict__ 
     while (g < groups) {
         const long long first = g * M;
         if (is_async(g)) {
-            if (!mbar_wait(bar, phase & 1u, kWaitLimit)) {
+            if (!mbar_wait(sm.bar, phase & 1u, kWaitLimit)) {
                 atomicOr(&g_device_error, 1);
                 break;
             }
@@ -676,196 +926,138 @@ __global__ void __launch_bounds__(256, 2) mi_inverse_kernel(float* __restrict__ 
         }
         __syncwarp();
 
-        // ---- pivot order (reference rules): groups of P lanes
-        if constexpr (MODE == kModeReference || MODE == kModeReferenceSerial) {
-            constexpr int GP = 32 / P;      // replay groups per warp
-            constexpr int IM = M / GP;      // matrices per replay group (= P / L)
-            const int gi = lane / P, sp = lane % P;
-            if constexpr (MODE == kModeReferenceSerial || (N & (N - 1)) == 0) {
-                const float* stm[IM];
-                int* winm[IM];
-#pragma unroll
-                for (int q = 0; q < IM; q++) {
-                    const int mm = q * GP + gi;
-                    stm[q] = slot + mm * G::kMat;
-                    winm[q] = reinterpret_cast<int*>(scr0 + mm * K::kScr + G::oWin);
-                }
-                replay_fast_multi<N, P, IM, MODE>(stm, winm, sp, gi * P);
-            } else {
-#pragma unroll 1
-                for (int q = 0; q < IM; ++q) {
-                    const int mm = q * GP + gi;
-                    replay_tracked<N, P, MODE>(slot + mm * G::kMat,
-                                               reinterpret_cast<int*>(scr0 + mm * K::kScr + G::oWin), sp, gi * P);
-                }
-            }
-        } else if constexpr (MODE == kModeNone) {
-            for (int t = s; t < N; t += L) win[t] = t;
-        }
-        __syncwarp();
-
-        // ---- register block, rows in pivot order
         float a[R][C];
-#pragma unroll
-        for (int ri = 0; ri < R; ri++) {
-            const int i = rg + G::RG * ri;
-            int src = i;
-            if constexpr (MODE == kModeReference || MODE == kModeReferenceSerial) src = (i < N) ? win[i] : 0;
-            if constexpr (N == 32 && C % 4 == 0) {
-#pragma unroll
-                for (int h = 0; h < C / 4; h++) {
-                    const int c0 = cg * C + 4 * h;
-                    const float4 v =
-                        *reinterpret_cast<const float4*>(st + src * 32 + ((((c0 >> 2) ^ (src & 7))) << 2));
-                    a[ri][4 * h] = v.x; a[ri][4 * h + 1] = v.y; a[ri][4 * h + 2] = v.z; a[ri][4 * h + 3] = v.w;
-                }
-                if (i >= N) {
-#pragma unroll
-                    for (int ci = 0; ci < C; ci++) a[ri][ci] = 0.0f;
-                }
-            } else {
-#pragma unroll
-                for (int ci = 0; ci < C; ci++) {
-                    const int j = cg * C + ci;
-                    a[ri][ci] = (i < N && j < N) ? st[stage_off<N>(src, j)] : 0.0f;
-                }
-            }
-        }
-        __syncwarp();
+        phase_load<N, L, MODE, (N == 32)>(a, sm.slot, sm.scr0, lane);
 
-        // ---- the slot is free: bring in this warp's next group now
+        // the slot is free: bring in this warp's next group now
         const long long gn = g + gstride;
         if (gn < groups) {
             if (lane == 0) fence_proxy_async();
             issue(gn);
         }
 
-        // ---- n elimination steps
-        float ps[R];
-#pragma unroll
-        for (int ri = 0; ri < R; ri++) ps[ri] = 1.0f;
-        if constexpr (MODE == kModePartial) {
-            int ra = s;
-#pragma unroll
-            for (int k = 0; k < N; ++k) gj_step_partial<G>(a, ps, k, rg, cg, s, mslot * L, scr, ra);
-            if (s < N) win[s] = ra;
-        } else {
-#pragma unroll
-            for (int k = 0; k < N; ++k) gj_step<G>(a, ps, k, rg, cg, mslot * L, scr);
-        }
-
-        // ---- scale each row by its 1/pivot
-#pragma unroll
-        for (int ri = 0; ri < R; ri++) {
-#pragma unroll
-            for (int q = 0; q < C / 2; q++) {
-                const float2 x =
-                    __fmul2_rn(make_float2(a[ri][2 * q], a[ri][2 * q + 1]), make_float2(ps[ri], ps[ri]));
-                a[ri][2 * q] = x.x;
-                a[ri][2 * q + 1] = x.y;
-            }
-        }
-        __syncwarp();
-
-        // ---- A^-1[i][win[j]] = X[i][j]: rows leave in rounds of ORows through
-        //      the row buffer (columns scattered there), then coalesced stores
-        int dst[C];
-#pragma unroll
-        for (int ci = 0; ci < C; ci++) {
-            const int j = cg * C + ci;
-            dst[ci] = (j < N) ? win[j] : 0;
-        }
+        phase_eliminate<N, L, MODE>(a, sm.scr0, lane);
         if (copy_mode == kCopyTensor) {
-#pragma unroll
-            for (int q = 0; q < K::Rounds; q++) {
-                float* obuf = outb + (q & 1) * K::kOutT;
-                float* ob = obuf + mslot * K::OBR * N;
-                if (lane == 0) bulk_wait_read_one();   // this buffer's store from two rounds ago has read it
-                __syncwarp();
-#pragma unroll
-                for (int h = 0; h < K::H; h++) {
-                    const int ri = q * K::H + h;
-                    const int lr = rg + G::RG * h;
-                    if (ri < R && lr < K::OBR) {
-                        const int i = rg + G::RG * ri;
-                        if (i < N) {
-                            float* orow = ob + lr * N;
-                            const int x = (N == 32) ? ((lr & 7) << 2) : 0;
-#pragma unroll
-                            for (int ci = 0; ci < C; ci++)
-                                if (cg * C + ci < N) orow[dst[ci] ^ x] = a[ri][ci];
-                        }
-                    }
-                }
-                fence_proxy_async();
-                __syncwarp();
-                if (lane == 0) {
-                    tma_store_3d(&tmap_out, 0, q * K::ORows, (int)first, obuf);
-                    bulk_commit();
-                }
-            }
+            phase_store_tensor<N, L, MODE>(a, sm.outb, sm.scr0, lane, &tmap_out, first);
         } else {
-            float* ob = outb + mslot * K::ORows * K::SB;
+            float* gout[M];
 #pragma unroll
-            for (int q = 0; q < K::Rounds; q++) {
-#pragma unroll
-                for (int h = 0; h < K::H; h++) {
-                    const int ri = q * K::H + h;
-                    if (ri < R) {
-                        const int i = rg + G::RG * ri;
-                        if (i < N) {
-                            float* orow = ob + (rg + G::RG * h) * K::SB;
-#pragma unroll
-                            for (int ci = 0; ci < C; ci++)
-                                if (cg * C + ci < N) orow[dst[ci]] = a[ri][ci];
-                        }
-                    }
-                }
-                __syncwarp();
-                const int row0 = q * K::ORows;
-                const int rows = (N - row0 < K::ORows) ? (N - row0) : K::ORows;
-                if (rows > 0) {
-                    if (vec_out && N % 4 == 0) {
-                        constexpr int Q = N / 4;               // 16-byte chunks per row
-                        const int per = rows * Q;
-                        for (int e = lane; e < M * per; e += 32) {
-                            const int m = e / per, rem = e - m * per;
-                            const int r = rem / Q, c4 = rem - r * Q;
-                            if (first + m < batch) {
-                                const float4 v =
-                                    *reinterpret_cast<const float4*>(outb + (m * K::ORows + r) * K::SB + 4 * c4);
-                                *reinterpret_cast<float4*>(A + (first + m) * NN + (row0 + r) * N + 4 * c4) = v;
-                            }
-                        }
-                    } else {
-                        const int per = rows * N;
-                        for (int e = lane; e < M * per; e += 32) {
-                            const int m = e / per, rem = e - m * per;
-                            const int r = rem / N, c = rem - r * N;
-                            if (first + m < batch)
-                                A[(first + m) * NN + (row0 + r) * N + c] = outb[(m * K::ORows + r) * K::SB + c];
-                        }
-                    }
-                }
-                __syncwarp();
-            }
+            for (int m = 0; m < M; m++) gout[m] = (first + m < batch) ? A + (first + m) * NN : nullptr;
+            phase_store_rows<N, L, MODE>(a, sm.outb, sm.scr0, lane, gout, vec_out != 0);
         }
-
-        // ---- perm and info (info: first step whose pivot was exactly zero)
         const long long mb = first + mslot;
-        unsigned zmask = 0u;
-#pragma unroll
-        for (int q = 0; q < (N + L - 1) / L; q++) {
-            const int t = s + q * L;
-            const bool z = (t < N) && (scr[G::oD + t] == 0.0f);
-            zmask |= group_ballot<L>(z, mslot * L) << (q * L);
-            if (perm_out != nullptr && t < N && mb < batch) perm_out[mb * N + t] = win[t];
-        }
-        if (info_out != nullptr && s == 0 && mb < batch) info_out[mb] = zmask ? __ffs(zmask) : 0;
-        __syncwarp();
+        phase_perm_info<N, L, MODE>(sm.scr0, lane, mb < batch ? mb : -1, perm_out, N, info_out);
         g = gn;
     }
     if (lane == 0) bulk_wait_all();
+}
+
+// ---------------------------------------------------------------------------
+// Indexed batch (descriptor buckets): the matrices of one (n, mode) bucket are
+// list[range[0] .. range[0] + range[1]) -- descriptor indices -- at
+// base + offsets[index].  Each matrix moves in by a 1-D bulk copy when its
+// address allows (16-byte aligned, n*n a multiple of 4), else element by
+// element with asynchronous copies; results leave with plain stores.  Pivots
+// go to perm_out[index * 32 ..], info to info_out[index].
+// ---------------------------------------------------------------------------
+template <int N, int L, int MODE>
+__global__ void __launch_bounds__(256, 2) mi_inverse_indexed_kernel(float* __restrict__ base,
+                                                                    const long long* __restrict__ offsets,
+                                                                    const int* __restrict__ list,
+                                                                    const long long* __restrict__ range,
+                                                                    int32_t* __restrict__ perm_out,
+                                                                    int32_t* __restrict__ info_out) {
+    using G = GeomN<N, L, MODE>;
+    using K = KGeom<N, L, MODE>;
+    constexpr int NN = N * N, R = G::R, C = G::C, M = G::M;
+    extern __shared__ unsigned char smem_raw[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int W = blockDim.x >> 5;
+    const WarpSmem<N, L, MODE> sm(smem_raw, warp);
+    const int mslot = lane / L;
+    const long long start = range[0], count = range[1];
+    if (count <= 0) return;
+
+    if (lane == 0) {
+        mbar_init(sm.bar, 1);
+        fence_mbar_init();
+    }
+    __syncwarp();
+    const bool base16 = (reinterpret_cast<uintptr_t>(base) & 15u) == 0;
+    const long long groups = (count + M - 1) / M;
+    const long long gstride = (long long)gridDim.x * W;
+
+    // descriptor index of matrix m of group g (-1 past the end of the bucket)
+    auto index_of = [&](long long g, int m) -> long long {
+        const long long p = g * M + m;
+        return p < count ? (long long)list[start + p] : -1;
+    };
+    auto bulk_ok = [&](long long idx) { return idx >= 0 && base16 && NN % 4 == 0 && (offsets[idx] & 3) == 0; };
+    // returns whether the group used the mbarrier
+    auto issue = [&](long long g) -> bool {
+        long long idx[M];
+        uint32_t bytes = 0;
+#pragma unroll
+        for (int m = 0; m < M; m++) {
+            idx[m] = index_of(g, m);
+            if (bulk_ok(idx[m])) bytes += NN * 4;
+        }
+        if (bytes != 0 && lane == 0) {
+            mbar_arrive_expect_tx(sm.bar, bytes);
+#pragma unroll
+            for (int m = 0; m < M; m++)
+                if (bulk_ok(idx[m])) bulk_load(sm.slot + m * G::kMat, base + offsets[idx[m]], NN * 4, sm.bar);
+        }
+#pragma unroll
+        for (int m = 0; m < M; m++) {
+            if (!bulk_ok(idx[m])) {
+                const bool valid = idx[m] >= 0;
+                const float* src = valid ? base + offsets[idx[m]] : base;
+                for (int e = lane; e < NN; e += 32)
+                    cp_async_4(sm.slot + m * G::kMat + e, valid ? src + e : base, valid);
+            }
+        }
+        cp_async_commit();
+        return bytes != 0;
+    };
+
+    long long g = (long long)blockIdx.x * W + warp;
+    uint32_t phase = 0;
+    bool used_bar = false;
+    if (g < groups) used_bar = issue(g);
+    while (g < groups) {
+        if (used_bar) {
+            if (!mbar_wait(sm.bar, phase & 1u, kWaitLimit)) {
+                atomicOr(&g_device_error, 1);
+                break;
+            }
+            phase++;
+        }
+        cp_async_wait_all();
+        __syncwarp();
+
+        float a[R][C];
+        phase_load<N, L, MODE, false>(a, sm.slot, sm.scr0, lane);
+
+        long long idx[M];
+        float* gout[M];
+        bool vec = base16 && N % 4 == 0;
+#pragma unroll
+        for (int m = 0; m < M; m++) {
+            idx[m] = index_of(g, m);
+            gout[m] = idx[m] >= 0 ? base + offsets[idx[m]] : nullptr;
+            if (idx[m] >= 0 && (offsets[idx[m]] & 3) != 0) vec = false;
+        }
+        const long long gn = g + gstride;
+        if (gn < groups) {
+            if (lane == 0) fence_proxy_async();
+            used_bar = issue(gn);
+        }
+        phase_eliminate<N, L, MODE>(a, sm.scr0, lane);
+        phase_store_rows<N, L, MODE>(a, sm.outb, sm.scr0, lane, gout, vec);
+        phase_perm_info<N, L, MODE>(sm.scr0, lane, idx[mslot], perm_out, 32, info_out);
+        g = gn;
+    }
 }
 
 // Dynamic shared memory for a block of `warps` warps (1 KB of slack for the

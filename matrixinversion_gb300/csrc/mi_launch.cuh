@@ -86,6 +86,44 @@ cudaError_t launch(float* a, int32_t* perm, int32_t* info, long long batch, int 
     return cudaGetLastError();
 }
 
+// Indexed bucket launch: the kernel reads its bucket's [start, count) from
+// `range` on the device, so the grid is fixed (persistent warps) and the
+// launch needs no host round trip -- it can be captured in a CUDA graph.
+using ilaunch_fn = cudaError_t (*)(float*, const long long*, const int*, const long long*, int32_t*, int32_t*, int,
+                                   int, cudaStream_t);
+
+template <int N, int MODE>
+cudaError_t launch_indexed(float* base, const long long* offsets, const int* list, const long long* range,
+                           int32_t* perm, int32_t* info, int tpb, int grid, cudaStream_t stream) {
+    constexpr int L = default_lanes(N, MODE);
+    const int warps = tpb / 32;
+    const size_t smem = smem_bytes<N, L, MODE>(warps);
+    auto kern = mi_inverse_indexed_kernel<N, L, MODE>;
+    static size_t smem_set = 0;
+    if (smem > 48 * 1024 && smem > smem_set) {
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        smem_set = smem;
+    }
+    if (grid <= 0) {
+        static int per_sm_cached[9] = {0};
+        int& per_sm = per_sm_cached[warps];
+        if (per_sm == 0) {
+            cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, tpb, smem);
+            if (e != cudaSuccess) return e;
+            if (per_sm < 1) per_sm = 1;
+        }
+        grid = per_sm * device_sm_count();
+    }
+    kern<<<grid, tpb, smem, stream>>>(base, offsets, list, range, perm, info);
+    return cudaGetLastError();
+}
+
+extern const ilaunch_fn kITableNone[33];
+extern const ilaunch_fn kITableReference[33];
+extern const ilaunch_fn kITableReferenceSerial[33];
+extern const ilaunch_fn kITablePartial[33];
+
 extern const launch_fn kTableNone[33];
 extern const launch_fn kTableReference[33];
 extern const launch_fn kTableReferenceSerial[33];
@@ -102,3 +140,15 @@ extern const launch_fn kTablePartial[33];
         launch<20, MODE>, launch<21, MODE>, launch<22, MODE>, launch<23, MODE>, launch<24, MODE>, \
         launch<25, MODE>, launch<26, MODE>, launch<27, MODE>, launch<28, MODE>, launch<29, MODE>, \
         launch<30, MODE>, launch<31, MODE>, launch<32, MODE>}
+
+#define MI_ITABLE(NAME, MODE)                                                                                 \
+    const ilaunch_fn NAME[33] = {                                                                             \
+        nullptr,                  launch_indexed<1, MODE>,  launch_indexed<2, MODE>,  launch_indexed<3, MODE>,  \
+        launch_indexed<4, MODE>,  launch_indexed<5, MODE>,  launch_indexed<6, MODE>,  launch_indexed<7, MODE>,  \
+        launch_indexed<8, MODE>,  launch_indexed<9, MODE>,  launch_indexed<10, MODE>, launch_indexed<11, MODE>, \
+        launch_indexed<12, MODE>, launch_indexed<13, MODE>, launch_indexed<14, MODE>, launch_indexed<15, MODE>, \
+        launch_indexed<16, MODE>, launch_indexed<17, MODE>, launch_indexed<18, MODE>, launch_indexed<19, MODE>, \
+        launch_indexed<20, MODE>, launch_indexed<21, MODE>, launch_indexed<22, MODE>, launch_indexed<23, MODE>, \
+        launch_indexed<24, MODE>, launch_indexed<25, MODE>, launch_indexed<26, MODE>, launch_indexed<27, MODE>, \
+        launch_indexed<28, MODE>, launch_indexed<29, MODE>, launch_indexed<30, MODE>, launch_indexed<31, MODE>, \
+        launch_indexed<32, MODE>}

@@ -1,0 +1,126 @@
+"""Mixed-size batches through an (offset, n, pivot flag) descriptor table.
+
+Matrix i of a packed float32 buffer starts at offsets[i] (floats) and is
+n_i x n_i, row-major; flags[i] is its pivot mode (0 none, 1 reference,
+2 reference_serial, 3 partial).  One call buckets the table by (n, flag) on
+the GPU and runs one persistent launch per bucket -- all stream-ordered, so
+the call can be captured into a CUDA graph (DescrGraph).
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib, pivot_mode
+
+
+def pack(matrices, align: int = 4):
+    """Pack host matrices (a list of square float32 arrays) back to back.
+
+    Each matrix starts on a multiple of `align` floats (4 = 16 bytes, which
+    lets the copies use the bulk copy engine; 1 = densely packed).  Returns
+    (packed float32[total], offsets int64[count], ns int32[count]).
+    """
+    ns = np.array([m.shape[0] for m in matrices], dtype=np.int32)
+    offsets = np.zeros(len(matrices), dtype=np.int64)
+    pos = 0
+    for i, m in enumerate(matrices):
+        pos = (pos + align - 1) // align * align
+        offsets[i] = pos
+        pos += m.shape[0] * m.shape[0]
+    packed = np.zeros(max(pos, 1), dtype=np.float32)
+    for i, m in enumerate(matrices):
+        k = m.shape[0]
+        packed[offsets[i]: offsets[i] + k * k] = np.asarray(m, dtype=np.float32).reshape(-1)
+    return packed, offsets, ns
+
+
+def unpack(packed, offsets, ns):
+    return [np.asarray(packed[o: o + n * n]).reshape(n, n) for o, n in zip(offsets, ns)]
+
+
+def workspace_bytes(count: int) -> int:
+    return int(_lib.load().mi_descr_workspace_bytes(int(count)))
+
+
+def masks(ns, flags) -> tuple[int, int]:
+    """(n_mask, mode_mask) covering the sizes and modes present."""
+    ns = np.asarray(ns)
+    flags = np.asarray(flags)
+    n_mask = 0
+    for n in np.unique(ns):
+        if 1 <= n <= 32:
+            n_mask |= 1 << (int(n) - 1)
+    mode_mask = 0
+    for f in np.unique(flags):
+        if 0 <= f <= 3:
+            mode_mask |= 1 << int(f)
+    return n_mask, mode_mask
+
+
+def batched_inverse_descr_(packed, offsets, ns, flags, *, perm=None, info=None, workspace=None, n_mask: int = 0,
+                           mode_mask: int = 0, stream=None):
+    """In-place inverse of every described matrix (CUDA tensors).
+
+    packed float32 [total]; offsets int64 [count]; ns, flags int32 [count];
+    perm int32 [count, 32] and info int32 [count] optional; workspace uint8
+    [workspace_bytes(count)] (allocated when None).  Returns (perm, info).
+    """
+    import torch
+
+    for name, t, dt in (("packed", packed, torch.float32), ("offsets", offsets, torch.int64),
+                        ("ns", ns, torch.int32), ("flags", flags, torch.int32)):
+        if not (isinstance(t, torch.Tensor) and t.is_cuda and t.dtype == dt and t.is_contiguous()):
+            raise TypeError(f"{name} must be a contiguous CUDA {dt} tensor")
+    count = offsets.numel()
+    if ns.numel() != count or flags.numel() != count:
+        raise ValueError("offsets, ns and flags must have the same length")
+    dev = packed.device
+    if workspace is None:
+        workspace = torch.empty(max(workspace_bytes(count), 256), dtype=torch.uint8, device=dev)
+    L = _lib.load()
+    st = (stream or torch.cuda.current_stream(dev)).cuda_stream
+    with torch.cuda.device(dev):
+        status = L.mi_inverse_descr_f32(
+            ctypes.c_void_p(packed.data_ptr()), ctypes.c_void_p(offsets.data_ptr()), ctypes.c_void_p(ns.data_ptr()),
+            ctypes.c_void_p(flags.data_ptr()), ctypes.c_void_p(perm.data_ptr() if perm is not None else 0),
+            ctypes.c_void_p(info.data_ptr() if info is not None else 0), count, n_mask & 0xFFFFFFFF,
+            mode_mask & 0xF, ctypes.c_void_p(workspace.data_ptr()), workspace.numel(), ctypes.c_void_p(st))
+    _lib.check(status)
+    return perm, info
+
+
+class DescrGraph:
+    """One descriptor call captured into a CUDA graph over fixed buffers.
+
+    Refill `packed` (and the descriptor tensors) in place, then `replay()`:
+    every bucket launch goes out as a single graph launch.
+    """
+
+    def __init__(self, packed, offsets, ns, flags, perm=None, info=None, n_mask: int = 0, mode_mask: int = 0):
+        import torch
+
+        self.args = (packed, offsets, ns, flags)
+        self.perm, self.info = perm, info
+        self.workspace = torch.empty(max(workspace_bytes(offsets.numel()), 256), dtype=torch.uint8,
+                                     device=packed.device)
+        self.masks = (n_mask, mode_mask)
+        self.stream = torch.cuda.Stream(device=packed.device)
+        # the first call sets kernel attributes and occupancy caches outside capture
+        scratch = packed.clone()
+        with torch.cuda.stream(self.stream):
+            batched_inverse_descr_(scratch, offsets, ns, flags, perm=perm, info=info, workspace=self.workspace,
+                                   n_mask=n_mask, mode_mask=mode_mask, stream=self.stream)
+        self.stream.synchronize()
+        del scratch
+        self.graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(self.graph, stream=self.stream):
+            batched_inverse_descr_(packed, offsets, ns, flags, perm=perm, info=info, workspace=self.workspace,
+                                   n_mask=n_mask, mode_mask=mode_mask, stream=self.stream)
+
+    def replay(self):
+        self.graph.replay()
+
+
+__all__ = ["pack", "unpack", "workspace_bytes", "masks", "batched_inverse_descr_", "DescrGraph", "pivot_mode"]

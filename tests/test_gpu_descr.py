@@ -1,0 +1,119 @@
+"""Descriptor batches (mixed n and pivot modes in one call) through the C ABI.
+
+Every matrix must come back bit-for-bit equal to the contiguous kernel's
+result for the same matrix (same arithmetic, different data movement), with
+the same pivots; malformed descriptors are reported and left untouched; the
+call replays correctly from a CUDA graph.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+MODES = ["none", "reference", "reference_serial", "partial"]
+
+
+def make_case(oracle, count, seed, nmin=1, nmax=32):
+    rng = np.random.RandomState(seed)
+    ns = rng.randint(nmin, nmax + 1, size=count)
+    flags = rng.randint(0, 4, size=count)
+    mats = []
+    for i, (n, f) in enumerate(zip(ns, flags)):
+        A = oracle.uniform(seed * 7919 + i, 1, int(n))[0]
+        if f == 0:
+            A = A + np.float32(n) * np.eye(n, dtype=np.float32)
+        mats.append(A)
+    return mats, ns.astype(np.int32), flags.astype(np.int32)
+
+
+def contiguous_results(mi, mats, flags):
+    import torch
+
+    out, perms, infos = [], [], []
+    for A, f in zip(mats, flags):
+        X, p, i = mi.batched_inverse(torch.from_numpy(A[None]).cuda(), MODES[f])
+        out.append(X[0].cpu().numpy())
+        perms.append(p[0].cpu().numpy())
+        infos.append(int(i[0].item()))
+    return out, perms, infos
+
+
+@pytest.mark.parametrize("align", [4, 1])
+def test_descriptor_batch_matches_contiguous(mi_gpu, oracle, align):
+    import torch
+
+    from matrixinversion_gb300 import descr
+
+    mats, ns, flags = make_case(oracle, 700, 3 + align)
+    packed, offsets, ns_ = descr.pack(mats, align=align)
+    d_packed = torch.from_numpy(packed).cuda()
+    perm = torch.full((len(mats), 32), -7, dtype=torch.int32, device="cuda")
+    info = torch.full((len(mats),), -7, dtype=torch.int32, device="cuda")
+    descr.batched_inverse_descr_(d_packed, torch.from_numpy(offsets).cuda(), torch.from_numpy(ns_).cuda(),
+                                 torch.from_numpy(flags).cuda(), perm=perm, info=info)
+    got = descr.unpack(d_packed.cpu().numpy(), offsets, ns_)
+    want, wperm, winfo = contiguous_results(mi_gpu, mats, flags)
+    perm = perm.cpu().numpy()
+    info = info.cpu().numpy()
+    for i, n in enumerate(ns_):
+        assert np.array_equal(got[i], want[i]), (i, n, flags[i])
+        assert np.array_equal(perm[i, :n], wperm[i]), i
+        assert info[i] == winfo[i]
+    # pivots of the reference rules against the oracle replay
+    for i, (A, f) in enumerate(zip(mats, flags)):
+        if f in (1, 2):
+            assert np.array_equal(perm[i, : A.shape[0]], oracle.pivots(A[None], MODES[f])[0])
+
+
+def test_malformed_descriptors_and_masks(mi_gpu, oracle):
+    import torch
+
+    from matrixinversion_gb300 import descr
+
+    mats, ns, flags = make_case(oracle, 40, 11, 2, 12)
+    packed, offsets, ns_ = descr.pack(mats)
+    bad_n = ns_.copy()
+    bad_n[3] = 0
+    bad_n[5] = 33
+    bad_f = flags.copy()
+    bad_f[7] = 9
+    d_packed = torch.from_numpy(packed).cuda()
+    info = torch.zeros(len(mats), dtype=torch.int32, device="cuda")
+    descr.batched_inverse_descr_(d_packed, torch.from_numpy(offsets).cuda(), torch.from_numpy(bad_n).cuda(),
+                                 torch.from_numpy(bad_f).cuda(), info=info)
+    info = info.cpu().numpy()
+    got = descr.unpack(d_packed.cpu().numpy(), offsets, ns_)
+    for i in (3, 5, 7):
+        assert info[i] == -1
+        assert np.array_equal(got[i], mats[i])        # untouched
+    want, _, _ = contiguous_results(mi_gpu, mats, flags)
+    assert np.array_equal(got[0], want[0])
+    # masks that exclude a present size leave those matrices untouched
+    d_packed = torch.from_numpy(packed).cuda()
+    n_mask, mode_mask = descr.masks(ns_, flags)
+    n_mask &= ~(1 << (int(ns_[0]) - 1))
+    descr.batched_inverse_descr_(d_packed, torch.from_numpy(offsets).cuda(), torch.from_numpy(ns_).cuda(),
+                                 torch.from_numpy(flags).cuda(), n_mask=n_mask, mode_mask=mode_mask)
+    got = descr.unpack(d_packed.cpu().numpy(), offsets, ns_)
+    assert np.array_equal(got[0], mats[0])
+
+
+def test_descriptor_graph_replay(mi_gpu, oracle):
+    import torch
+
+    from matrixinversion_gb300 import descr
+
+    mats, ns, flags = make_case(oracle, 300, 21)
+    packed, offsets, ns_ = descr.pack(mats)
+    d_packed = torch.from_numpy(packed).cuda()
+    n_mask, mode_mask = descr.masks(ns_, flags)
+    g = descr.DescrGraph(d_packed, torch.from_numpy(offsets).cuda(), torch.from_numpy(ns_).cuda(),
+                         torch.from_numpy(flags).cuda(), n_mask=n_mask, mode_mask=mode_mask)
+    want, _, _ = contiguous_results(mi_gpu, mats, flags)
+    for _ in range(2):
+        d_packed.copy_(torch.from_numpy(packed))
+        g.replay()
+        torch.cuda.synchronize()
+        got = descr.unpack(d_packed.cpu().numpy(), offsets, ns_)
+        for i in range(len(mats)):
+            assert np.array_equal(got[i], want[i]), i
