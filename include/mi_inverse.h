@@ -53,6 +53,7 @@ extern "C" {
 #define MI_ERR_NULL_POINTER (-2)  /* d_a is NULL while batch > 0 */
 #define MI_ERR_MISALIGNED (-3)    /* d_a not 4-byte aligned */
 #define MI_ERR_CUDA (-4)          /* a CUDA call failed; see mi_last_cuda_error() */
+#define MI_ERR_SCRATCH_LIMIT (-5) /* count above MI_NOALLOC_MAX_COUNT (no-allocation entry point) */
 
 /* pivot modes */
 #define MI_PIVOT_NONE 0             /* plain LU (templated/ kernel)                  */
@@ -106,6 +107,36 @@ int mi_inverse_descr_f32(float* d_packed, const int64_t* d_offsets, const int32_
                          int32_t* d_perm, int32_t* d_info, int64_t count, uint32_t n_mask, uint32_t mode_mask,
                          void* d_workspace, size_t workspace_bytes, void* stream);
 size_t mi_descr_workspace_bytes(int64_t count);
+
+/*
+ * mi_inverse_descr_f32 without a caller workspace -- no counterpart in the
+ * reference, whose kernels need no scratch.  For callers that cannot
+ * allocate device memory when they invert: a serving loop whose HBM is
+ * carved up once at start-up under a fixed budget, code whose framework
+ * allocator must see every device allocation, and latency-bound loops --
+ * cudaMalloc and cudaFree synchronise the device and stall every stream.
+ * The bucketing scratch is a fixed file-scope device array of
+ * 4096 + 4 * MI_NOALLOC_MAX_COUNT bytes (about 1 MB) per device; the call
+ * itself allocates nothing.
+ *   count > MI_NOALLOC_MAX_COUNT  returns MI_ERR_SCRATCH_LIMIT and launches
+ *                 nothing; use mi_inverse_descr_f32 with your own workspace.
+ *   First call on each device: looks up the scratch's device address
+ *                 (cudaGetSymbolAddress, with that device current), which also
+ *                 loads the library's device code there if needed.  Make that
+ *                 first call before any stream capture begins.
+ *   Zeroing:      the caller clears nothing; each call resets the scratch's
+ *                 bucket counters on `stream` before use, and the rest of the
+ *                 scratch is written before it is read.
+ *   Concurrency:  one scratch per device, so calls that overlap on the same
+ *                 device (other streams or host threads, not ordered by the
+ *                 same stream or by events) race on it and can return wrong
+ *                 results.  Order them.
+ * Arguments, results and other status codes as mi_inverse_descr_f32.
+ */
+#define MI_NOALLOC_MAX_COUNT 262144
+int mi_inverse_descr_noalloc_f32(float* d_packed, const int64_t* d_offsets, const int32_t* d_n,
+                                 const int32_t* d_flags, int32_t* d_perm, int32_t* d_info, int64_t count,
+                                 uint32_t n_mask, uint32_t mode_mask, void* stream);
 
 /* Threads per block used for size n and pivot mode (0 = built-in default). */
 int mi_set_launch_config(int n, int pivot, int threads_per_block);

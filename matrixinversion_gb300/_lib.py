@@ -15,6 +15,8 @@ MI_ERR_INVALID_VALUE = -1
 MI_ERR_NULL_POINTER = -2
 MI_ERR_MISALIGNED = -3
 MI_ERR_CUDA = -4
+MI_ERR_SCRATCH_LIMIT = -5
+MI_NOALLOC_MAX_COUNT = 262144
 
 PIVOT_MODES = {"none": 0, "reference": 1, "reference_serial": 2, "partial": 3}
 
@@ -58,6 +60,8 @@ def load(path: str | None = None):
     L.mi_inverse_descr_f32.argtypes = [vp, vp, vp, vp, vp, vp, i64, ctypes.c_uint32, ctypes.c_uint32, vp,
                                        ctypes.c_size_t, vp]
     L.mi_inverse_descr_f32.restype = i32
+    L.mi_inverse_descr_noalloc_f32.argtypes = [vp, vp, vp, vp, vp, vp, i64, ctypes.c_uint32, ctypes.c_uint32, vp]
+    L.mi_inverse_descr_noalloc_f32.restype = i32
     L.mi_descr_workspace_bytes.argtypes = [i64]
     L.mi_descr_workspace_bytes.restype = ctypes.c_size_t
     L.mi_set_launch_config.argtypes = [i32, i32, i32]
@@ -88,6 +92,7 @@ def exported_symbols() -> list[str]:
         "mi_abi_version",
         "mi_inverse_descr_f32",
         "mi_descr_workspace_bytes",
+        "mi_inverse_descr_noalloc_f32",
         "mi_set_launch_config",
         "mi_get_launch_config",
     ]

@@ -87,6 +87,7 @@ const char* mi_error_string(int status) {
         case MI_ERR_NULL_POINTER: return "null matrix pointer with batch > 0";
         case MI_ERR_MISALIGNED: return "matrix pointer is not 4-byte aligned";
         case MI_ERR_CUDA: return "CUDA error (see mi_last_cuda_error)";
+        case MI_ERR_SCRATCH_LIMIT: return "descriptor count above MI_NOALLOC_MAX_COUNT (262144) for the no-allocation entry point";
         default: return "unknown status";
     }
 }
