@@ -60,7 +60,7 @@
 namespace mi {
 
 enum : int { kModeNone = 0, kModeReference = 1, kModeReferenceSerial = 2, kModePartial = 3 };
-enum : int { kCopyPlain = 0, kCopyBulk = 1, kCopyTensor = 2 };
+enum : int { kCopyPlain = 0, kCopyBulk = 1, kCopyTensor = 2, kCopyWindow = 3 };
 
 constexpr unsigned kFull = 0xffffffffu;
 // Longest wait for one tile copy (SM clocks, about 2 s) before the kernel
@@ -309,15 +309,37 @@ __device__ __forceinline__ void load_keys4(const float* st, int r, int k0, unsig
     }
 }
 
+// Maximum over the P-lane group that starts at lane gbase: one warp
+// reduction, each group naming its own lanes.
+// Groups of 8 or fewer lanes use a shuffle butterfly instead (reductions over
+// several disjoint lane masks in one instruction were measured slower there).
+template <int P>
+__device__ __forceinline__ unsigned group_max_redux(unsigned x, int gbase) {
+    if constexpr (P == 32) return __reduce_max_sync(kFull, x);
+    else if constexpr (P >= 16) return __reduce_max_sync(((1u << P) - 1u) << gbase, x);
+    else return group_max<P>(x);
+}
+
 // The fast replay for IM matrices at once, one independent chain each, so
 // the reduction latencies of the chains overlap; keys are read from the
-// stage four columns at a time (a compact, rolled loop).
+// stage four columns at a time (a compact, rolled loop).  A step costs one
+// group maximum: the lane holding it takes the step, with no per-step vote or
+// branch.  A matrix whose maximum ever tied (two rows placed in one step,
+// so a later step finds only placed rows, key 0, and they take it again) or
+// where a NaN competed is replayed afterwards with the exact rule.
 template <int N, int P, int IM, int MODE, bool SW = (N == 32)>
 __device__ __forceinline__ void replay_fast_multi(const float* const (&st)[IM], int* const (&win)[IM], int s,
                                                   int gbase) {
-    bool placed[IM];
+    bool placed[IM], dup[IM];
+    int step[IM];
+    unsigned top[IM];
 #pragma unroll
-    for (int m = 0; m < IM; m++) placed[m] = (s >= N);
+    for (int m = 0; m < IM; m++) {
+        placed[m] = (s >= N);
+        dup[m] = false;
+        step[m] = 0;
+        top[m] = 0u;
+    }
 #pragma unroll 1
     for (int k0 = 0; k0 < N; k0 += 4) {
         unsigned kv[IM][4];
@@ -327,28 +349,30 @@ __device__ __forceinline__ void replay_fast_multi(const float* const (&st)[IM], 
         for (int t = 0; t < 4; t++) {
             const int k = k0 + t;
             if (N % 4 == 0 || k < N) {
-                unsigned tb[IM];
-                bool rare = false;
 #pragma unroll
                 for (int m = 0; m < IM; m++) {
                     const unsigned cand = placed[m] ? 0u : kv[m][t];
-                    const unsigned mx = group_max<P>(cand);
-                    tb[m] = group_ballot<P>(cand == mx, gbase);
-                    rare = rare || ((tb[m] & (tb[m] - 1u)) != 0u) || (mx > 0x7f800000u);
+                    const unsigned mx = group_max_redux<P>(cand, gbase);
+                    const bool hit = (cand == mx);
+                    dup[m] = dup[m] || (hit && placed[m]);
+                    top[m] = max(top[m], mx);
+                    if (hit) {
+                        placed[m] = true;
+                        step[m] = k;
+                    }
                 }
-                int w[IM];
-                if (__any_sync(kFull, rare)) {
+            }
+        }
+    }
 #pragma unroll
-                    for (int m = 0; m < IM; m++) w[m] = exact_pivot<N, P, MODE, SW>(st[m], win[m], k, s, gbase);
-                } else {
-#pragma unroll
-                    for (int m = 0; m < IM; m++) w[m] = __ffs(tb[m]) - 1;
-                }
-#pragma unroll
-                for (int m = 0; m < IM; m++) {
-                    if (s == w[m]) placed[m] = true;
-                    if (s == 0) win[m][k] = w[m];
-                }
+    for (int m = 0; m < IM; m++) {
+        const bool bad = (group_ballot<P>(dup[m], gbase) != 0u) || (top[m] > 0x7f800000u);
+        if (!bad && s < N) win[m][step[m]] = s;
+        if (__any_sync(kFull, bad)) {
+#pragma unroll 1
+            for (int k = 0; k < N; ++k) {
+                const int w = exact_pivot<N, P, MODE, SW>(st[m], win[m], k, s, gbase);
+                if (bad && s == 0) win[m][k] = w;
             }
         }
     }
@@ -357,7 +381,7 @@ __device__ __forceinline__ void replay_fast_multi(const float* const (&st)[IM], 
 // Non-power-of-two n under the reference rule: some tree slots are dropped,
 // so positions are tracked every step (lane = row).
 template <int N, int P, int MODE, bool SW = (N == 32)>
-__device__ __forceinline__ void replay_tracked(const float* st, int* win, int s, int gbase) {
+__device__ __noinline__ void replay_tracked(const float* st, int* win, int s, int gbase) {
     constexpr unsigned kSurv = survive_mask(N);
     unsigned key[N];
 #pragma unroll
@@ -386,6 +410,64 @@ __device__ __forceinline__ void replay_tracked(const float* st, int* win, int s,
         if (s == wl) pos = k;
         else if (pos == k) pos = pw;
         if (s == 0) win[k] = wl;
+    }
+}
+
+// The tracked replay for IM matrices at once (independent chains that
+// overlap).  Per step and matrix: the diagonal key and the winner's position
+// are broadcast by group maxima (only one lane contributes a non-zero value),
+// and each lane records the step at which it is placed.  Ties between the
+// surviving candidates are only flagged here; a matrix with a tie is replayed
+// again by replay_tracked, which applies the tree's tie order.
+template <int N, int P, int IM, int MODE, bool SW = (N == 32)>
+__device__ __forceinline__ void replay_tracked_multi(const float* const (&st)[IM], int* const (&win)[IM], int s,
+                                                     int gbase) {
+    constexpr unsigned kSurv = survive_mask(N);
+    unsigned key[IM][N];
+#pragma unroll
+    for (int m = 0; m < IM; m++)
+#pragma unroll
+        for (int k = 0; k < N; k++) key[m][k] = (s < N) ? pivot_key(st[m][stage_off<N, SW>(s, k)]) : 0u;
+    int pos[IM], step[IM];
+    unsigned tie[IM];
+#pragma unroll
+    for (int m = 0; m < IM; m++) {
+        pos[m] = (s < N) ? s : 0x7fff;
+        step[m] = 0;
+        tie[m] = 0u;
+    }
+#pragma unroll
+    for (int k = 0; k < N; ++k) {
+#pragma unroll
+        for (int m = 0; m < IM; m++) {
+            const bool at = (pos[m] == k);
+            unsigned kd;
+            if constexpr (P == 32) {
+                kd = __reduce_max_sync(kFull, at ? key[m][k] : 0u);
+            } else {
+                const int dl = __ffs(group_ballot<P>(at, gbase)) - 1;
+                kd = __shfl_sync(kFull, key[m][k], gbase + dl);
+            }
+            const int slot = pos[m] - k - 1;
+            const bool ok = (slot >= 0) && (pos[m] < N) && (key[m][k] > kd) && (key[m][k] <= 0x7f800000u) &&
+                            ((kSurv >> (slot & 31)) & 1u);
+            const unsigned cand = ok ? key[m][k] : 0u;
+            const unsigned mx = (P == 32) ? __reduce_max_sync(kFull, cand) : group_max<P>(cand);
+            const bool hit = ok && (cand == mx);
+            const unsigned tb = group_ballot<P>(hit, gbase);
+            tie[m] |= tb & (tb - 1u);
+            int wpos;
+            if constexpr (P == 32) wpos = (int)__reduce_max_sync(kFull, hit ? (unsigned)pos[m] : 0u);
+            else wpos = __shfl_sync(kFull, pos[m], gbase + (tb ? __ffs(tb) - 1 : 0));
+            if (hit || (at && mx == 0u)) step[m] = k;
+            if (hit) pos[m] = k;
+            else if (at && mx != 0u) pos[m] = wpos;
+        }
+    }
+#pragma unroll
+    for (int m = 0; m < IM; m++) {
+        if (tie[m] == 0u && s < N) win[m][step[m]] = s;
+        if (__any_sync(kFull, tie[m] != 0u)) replay_tracked<N, P, MODE, SW>(st[m], win[m], s, gbase);
     }
 }
 
@@ -566,14 +648,25 @@ struct KGeom {
     static constexpr int kSlot = G::M * G::kMat;
     static constexpr int kOutT = G::M * OBR * N;                  // one tensor-store buffer
     static constexpr int kOutS = G::M * ORows * SB;
-    static constexpr int kOut = (2 * kOutT > kOutS) ? 2 * kOutT : kOutS;
+    // Window copies (n not a multiple of 4): the group arrives as one 1-D bulk
+    // copy of the 16-byte-aligned window around it (up to 3 floats of shift
+    // and 3 of rounding), and each output round of a matrix leaves from a
+    // region placed at the same shift as its global range.
+    // Measured on GB300 (1,000,000 matrices): the window store wins from
+    // n = 10 up in the reference and no-pivot modes; below that, and in
+    // partial mode, the rows leave faster by coalesced plain stores.
+    static constexpr bool WinStore = (N % 4 != 0) && (N >= 10) && (MODE != kModePartial);
+    static constexpr int kOWm = (ORows * N + 3 + 3) & ~3;
+    static constexpr int kOutW = G::M * kOWm;
+    static constexpr int kOut0 = (2 * kOutT > kOutS) ? 2 * kOutT : kOutS;
+    static constexpr int kOut = (WinStore && 2 * kOutW > kOut0) ? 2 * kOutW : kOut0;
     static constexpr int kScr = (MODE == kModePartial) ? G::kScratch : 64;   // partial needs the exchange buffers
     static constexpr int kScrTotal = G::M * kScr;
     static constexpr int r4(int x) { return (x + 3) & ~3; }
     // per-warp region (floats): slot | output rows | scratch | mbarrier; the
     // output buffers start on a 128-byte boundary (1 KB for n = 32, where one
     // buffer is a multiple of 1 KB)
-    static constexpr int oOut = (N == 32) ? ((kSlot + 255) & ~255) : ((kSlot + 31) & ~31);
+    static constexpr int oOut = (N == 32) ? ((kSlot + 255) & ~255) : ((kSlot + 8 + 31) & ~31);
     static constexpr int oScr = oOut + r4(kOut);
     static constexpr int oBar = oScr + r4(kScrTotal);
     static constexpr int kWarp = (oBar + 4 + 255) / 256 * 256;   // 1 KB multiple
@@ -629,12 +722,15 @@ __device__ __forceinline__ void phase_load(float (&a)[GeomN<N, L, MODE>::R][Geom
             }
             replay_fast_multi<N, P, IM, MODE, SW>(stm, winm, sp, gi * P);
         } else {
-#pragma unroll 1
-            for (int q = 0; q < IM; ++q) {
+            const float* stm[IM];
+            int* winm[IM];
+#pragma unroll
+            for (int q = 0; q < IM; q++) {
                 const int mm = q * GP + gi;
-                replay_tracked<N, P, MODE, SW>(slot + mm * G::kMat,
-                                               reinterpret_cast<int*>(scr0 + mm * K::kScr + G::oWin), sp, gi * P);
+                stm[q] = slot + mm * G::kMat;
+                winm[q] = reinterpret_cast<int*>(scr0 + mm * K::kScr + G::oWin);
             }
+            replay_tracked_multi<N, P, IM, MODE, SW>(stm, winm, sp, gi * P);
         }
     } else if constexpr (MODE == kModeNone) {
         for (int t = s; t < N; t += L) win[t] = t;
@@ -722,7 +818,7 @@ __device__ __forceinline__ void dest_columns(int (&dst)[GeomN<N, L, MODE>::C], c
 template <int N, int L, int MODE>
 __device__ __forceinline__ void phase_store_tensor(const float (&a)[GeomN<N, L, MODE>::R][GeomN<N, L, MODE>::C],
                                                    float* outb, const float* scr0, int lane, const CUtensorMap* tmap_out,
-                                                   long long first) {
+                                                   long long first, unsigned& round) {
     using G = GeomN<N, L, MODE>;
     using K = KGeom<N, L, MODE>;
     constexpr int R = G::R, C = G::C;
@@ -732,7 +828,11 @@ __device__ __forceinline__ void phase_store_tensor(const float (&a)[GeomN<N, L, 
     dest_columns<N, L, MODE>(dst, scr0, lane);
 #pragma unroll
     for (int q = 0; q < K::Rounds; q++) {
-        float* obuf = outb + (q & 1) * K::kOutT;
+        // buffers alternate over the warp's whole sequence of rounds, so the
+        // one written now is never the one of the most recent store (with an
+        // even number of rounds per group that is the round's own parity)
+        const unsigned par = (K::Rounds & 1) ? ((round + q) & 1u) : ((unsigned)q & 1u);
+        float* obuf = outb + par * K::kOutT;
         float* ob = obuf + mslot * K::OBR * N;
         if (lane == 0) bulk_wait_read_one();   // this buffer's store from two rounds ago has read it
         __syncwarp();
@@ -758,6 +858,78 @@ __device__ __forceinline__ void phase_store_tensor(const float (&a)[GeomN<N, L, 
             bulk_commit();
         }
     }
+    round += K::Rounds;
+}
+
+// ---- phase C3 (n not a multiple of 4, 16-byte aligned batch): each output
+// round of matrix m is the contiguous range [G0, G1) of A.  Its rows are
+// written to a region at the shift G0 mod 4, the 16-byte-aligned interior
+// leaves by a 1-D bulk store, and the at most 3 + 3 floats outside it by
+// plain stores.  Buffers alternate over the warp's sequence of rounds.
+template <int N, int L, int MODE>
+__device__ __forceinline__ void phase_store_window(const float (&a)[GeomN<N, L, MODE>::R][GeomN<N, L, MODE>::C],
+                                                   float* outb, const float* scr0, int lane, float* A,
+                                                   long long first, long long batch, unsigned& round) {
+    using G = GeomN<N, L, MODE>;
+    using K = KGeom<N, L, MODE>;
+    constexpr int R = G::R, C = G::C, M = G::M;
+    constexpr long long NN = (long long)N * N;
+    const int mslot = lane / L, s = lane % L;
+    const int rg = s % G::RG, cg = s / G::RG;
+    int dst[C];
+    dest_columns<N, L, MODE>(dst, scr0, lane);
+#pragma unroll
+    for (int q = 0; q < K::Rounds; q++) {
+        const int row0 = q * K::ORows;
+        const int rows = (N - row0 < K::ORows) ? (N - row0) : K::ORows;
+        const unsigned par = (K::Rounds & 1) ? ((round + q) & 1u) : ((unsigned)q & 1u);
+        float* obuf = outb + par * K::kOutW;
+        if (lane == 0) bulk_wait_read_one();
+        __syncwarp();
+        const int e = (int)(((first + mslot) * NN + (long long)row0 * N) & 3);
+        float* ob = obuf + mslot * K::kOWm + e;
+#pragma unroll
+        for (int h = 0; h < K::H; h++) {
+            const int ri = q * K::H + h;
+            if (ri < R) {
+                const int i = rg + G::RG * ri;
+                if (i < N) {
+                    float* orow = ob + (rg + G::RG * h) * N;
+#pragma unroll
+                    for (int ci = 0; ci < C; ci++)
+                        if (cg * C + ci < N) orow[dst[ci]] = a[ri][ci];
+                }
+            }
+        }
+        fence_proxy_async();
+        __syncwarp();
+        if (lane == 0) {
+#pragma unroll
+            for (int m = 0; m < M; m++) {
+                if (first + m < batch) {
+                    const long long g0 = (first + m) * NN + (long long)row0 * N, g1 = g0 + (long long)rows * N;
+                    const long long a0 = (g0 + 3) & ~3LL, a1 = g1 & ~3LL;
+                    if (a1 > a0)
+                        bulk_store(A + a0, obuf + m * K::kOWm + (int)(g0 & 3) + (int)(a0 - g0),
+                                   (uint32_t)((a1 - a0) * 4));
+                }
+            }
+            bulk_commit();
+        }
+        for (int t = lane; t < M * 6; t += 32) {
+            const int m = t / 6, u = t - m * 6;
+            if (first + m < batch) {
+                const long long g0 = (first + m) * NN + (long long)row0 * N, g1 = g0 + (long long)rows * N;
+                const long long a0 = (g0 + 3) & ~3LL, a1 = g1 & ~3LL;
+                const long long head_end = a0 < g1 ? a0 : g1;
+                const long long x = (u < 3) ? g0 + u : ((a1 > a0 ? a1 : a0) + (u - 3));
+                const bool valid = (u < 3) ? (x < head_end) : (x < g1);
+                if (valid) A[x] = obuf[m * K::kOWm + (int)(g0 & 3) + (int)(x - g0)];
+            }
+        }
+        __syncwarp();
+    }
+    round += K::Rounds;
 }
 
 // ---- phase C2: rows leave through one padded buffer with plain stores to the
@@ -888,16 +1060,34 @@ __global__ void __launch_bounds__(256, 2) mi_inverse_kernel(float* __restrict__ 
 
     const long long groups = (batch + M - 1) / M;
     const long long gstride = (long long)gridDim.x * W;
+    // window copies: the 16-byte-aligned float range [w0, w1) around the group,
+    // used while it stays inside the batch
+    auto window = [&](long long g, long long& w0, long long& w1) {
+        const long long f0 = g * M * NN;
+        const long long cnt = (batch - g * M < M) ? (batch - g * M) : M;
+        w0 = f0 & ~3LL;
+        w1 = (f0 + cnt * NN + 3) & ~3LL;
+        return w1 <= batch * NN;
+    };
     auto is_async = [&](long long g) {
-        return copy_mode == kCopyTensor || (copy_mode == kCopyBulk && (g + 1) * M <= batch);
+        long long w0, w1;
+        return copy_mode == kCopyTensor || (copy_mode == kCopyBulk && (g + 1) * M <= batch) ||
+               (copy_mode == kCopyWindow && window(g, w0, w1));
     };
     auto issue = [&](long long g) {
         const long long first = g * M;
         if (is_async(g)) {
             if (lane == 0) {
-                mbar_arrive_expect_tx(sm.bar, (uint32_t)(K::kSlot * 4));
-                if (copy_mode == kCopyTensor) tma_load_3d(sm.slot, &tmap, 0, 0, (int)first, sm.bar);
-                else bulk_load(sm.slot, A + first * NN, (uint32_t)(K::kSlot * 4), sm.bar);
+                if (copy_mode == kCopyWindow) {
+                    long long w0, w1;
+                    window(g, w0, w1);
+                    mbar_arrive_expect_tx(sm.bar, (uint32_t)((w1 - w0) * 4));
+                    bulk_load(sm.slot, A + w0, (uint32_t)((w1 - w0) * 4), sm.bar);
+                } else {
+                    mbar_arrive_expect_tx(sm.bar, (uint32_t)(K::kSlot * 4));
+                    if (copy_mode == kCopyTensor) tma_load_3d(sm.slot, &tmap, 0, 0, (int)first, sm.bar);
+                    else bulk_load(sm.slot, A + first * NN, (uint32_t)(K::kSlot * 4), sm.bar);
+                }
             }
         } else {
             for (int e = lane; e < M * NN; e += 32) {
@@ -912,10 +1102,14 @@ __global__ void __launch_bounds__(256, 2) mi_inverse_kernel(float* __restrict__ 
 
     long long g = (long long)blockIdx.x * W + warp;
     uint32_t phase = 0;
+    unsigned round = 0;
     if (g < groups) issue(g);
     while (g < groups) {
         const long long first = g * M;
-        if (is_async(g)) {
+        const bool async_g = is_async(g);
+        // a window copy lands at the group's offset within its 16-byte granule
+        const int shift = (copy_mode == kCopyWindow && async_g) ? (int)((first * NN) & 3) : 0;
+        if (async_g) {
             if (!mbar_wait(sm.bar, phase & 1u, kWaitLimit)) {
                 atomicOr(&g_device_error, 1);
                 break;
@@ -927,7 +1121,7 @@ __global__ void __launch_bounds__(256, 2) mi_inverse_kernel(float* __restrict__ 
         __syncwarp();
 
         float a[R][C];
-        phase_load<N, L, MODE, (N == 32)>(a, sm.slot, sm.scr0, lane);
+        phase_load<N, L, MODE, (N == 32)>(a, sm.slot + shift, sm.scr0, lane);
 
         // the slot is free: bring in this warp's next group now
         const long long gn = g + gstride;
@@ -938,7 +1132,9 @@ __global__ void __launch_bounds__(256, 2) mi_inverse_kernel(float* __restrict__ 
 
         phase_eliminate<N, L, MODE>(a, sm.scr0, lane);
         if (copy_mode == kCopyTensor) {
-            phase_store_tensor<N, L, MODE>(a, sm.outb, sm.scr0, lane, &tmap_out, first);
+            phase_store_tensor<N, L, MODE>(a, sm.outb, sm.scr0, lane, &tmap_out, first, round);
+        } else if (K::WinStore && copy_mode == kCopyWindow) {
+            phase_store_window<N, L, MODE>(a, sm.outb, sm.scr0, lane, A, first, batch, round);
         } else {
             float* gout[M];
 #pragma unroll

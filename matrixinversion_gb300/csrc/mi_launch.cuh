@@ -65,6 +65,8 @@ cudaError_t launch(float* a, int32_t* perm, int32_t* info, long long batch, int 
         if (N % 4 == 0 && batch <= 0x7fffffffLL && make_tensor_map(&map, a, N, batch, N, G::M) &&
             make_tensor_map(&map_out, a, N, batch, KGeom<N, L, MODE>::OBR, G::M))
             copy_mode = kCopyTensor;
+        else if (N % 4 != 0)
+            copy_mode = kCopyWindow;
         else if (((long long)G::M * N * N) % 4 == 0)
             copy_mode = kCopyBulk;
     }

@@ -226,3 +226,38 @@ def test_cublas_comparator_is_an_inverse(mi_gpu, oracle):
     assert (info.cpu().numpy() == 0).all() and t1 > 0 and t2 > 0
     rel = np.abs(C.cpu().numpy() - X64).max((1, 2)) / np.abs(X64).max((1, 2))
     assert np.median(rel) < 1e-4
+
+
+@pytest.mark.parametrize("n", [3, 5, 10, 13, 17, 25, 31])
+@pytest.mark.parametrize("mode", ["none", "reference", "partial"])
+def test_copy_paths_keep_neighbours_and_agree(mi_gpu, oracle, n, mode):
+    """A batch placed inside a larger buffer: 16-byte-aligned starts take the
+    windowed bulk copies (n not a multiple of 4), a 4-byte offset the plain
+    copies.  Floats outside the batch must be untouched, and every copy path
+    must give the same bits."""
+    import torch
+
+    sentinel = np.float32(12345.5)
+    for batch in (1, 2, 3, 5, 17, 64, 129):
+        A = oracle.uniform(70 + batch, batch, n)
+        if mode == "none":
+            A = A + np.float32(n) * np.eye(n, dtype=np.float32)
+        results = []
+        for off in (0, 4, 8, 1):
+            total = off + batch * n * n + 11
+            buf = torch.full((total,), float(sentinel), dtype=torch.float32, device="cuda")
+            buf[off: off + batch * n * n] = torch.from_numpy(A.reshape(-1)).cuda()
+            view = buf[off: off + batch * n * n].view(batch, n, n)
+            mi_gpu.batched_inverse_(view, mode)
+            torch.cuda.synchronize()
+            h = buf.cpu().numpy()
+            assert np.all(h[:off] == sentinel) and np.all(h[off + batch * n * n:] == sentinel), (batch, off)
+            results.append(h[off: off + batch * n * n].copy())
+        for r in results[1:]:
+            assert np.array_equal(r, results[0]), batch
+        X = results[0].reshape(batch, n, n)
+        if mode != "none":          # per-matrix bound only: a median of a few matrices means nothing
+            bound, _ = residual_bound(oracle, A, mode)
+            assert np.all(oracle.residual(A, X)[:, 0] <= bound)
+        else:
+            assert np.all(oracle.residual(A, X)[:, 0] < 1e-5)
