@@ -414,60 +414,64 @@ __device__ __noinline__ void replay_tracked(const float* st, int* win, int s, in
 }
 
 // The tracked replay for IM matrices at once (independent chains that
-// overlap).  Per step and matrix: the diagonal key and the winner's position
-// are broadcast by group maxima (only one lane contributes a non-zero value),
-// and each lane records the step at which it is placed.  Ties between the
-// surviving candidates are only flagged here; a matrix with a tie is replayed
-// again by replay_tracked, which applies the tree's tie order.
+// overlap).  Keys are encoded 2|x| for a candidate and 2|x| + 1 for the row on
+// the diagonal, so one group maximum decides the step: an odd maximum means
+// no surviving candidate beats the diagonal strictly (it stays), an even one
+// names the winner.  A second maximum brings the winner's position to the
+// row it displaces.  Lanes record the step at which they are placed.  Ties
+// between candidates and NaNs that take part (codes above 2 * inf + 1) are
+// only flagged here; such a matrix is replayed again by replay_tracked.
 template <int N, int P, int IM, int MODE, bool SW = (N == 32)>
 __device__ __forceinline__ void replay_tracked_multi(const float* const (&st)[IM], int* const (&win)[IM], int s,
                                                      int gbase) {
     constexpr unsigned kSurv = survive_mask(N);
-    unsigned key[IM][N];
+    constexpr unsigned kInfCode = 0x7f800000u << 1;
+    unsigned ek[IM][N];
 #pragma unroll
     for (int m = 0; m < IM; m++)
 #pragma unroll
-        for (int k = 0; k < N; k++) key[m][k] = (s < N) ? pivot_key(st[m][stage_off<N, SW>(s, k)]) : 0u;
+        for (int k = 0; k < N; k++) ek[m][k] = (s < N) ? (pivot_key(st[m][stage_off<N, SW>(s, k)]) << 1) : 0u;
     int pos[IM], step[IM];
-    unsigned tie[IM];
+    unsigned tie[IM], top[IM];
 #pragma unroll
     for (int m = 0; m < IM; m++) {
-        pos[m] = (s < N) ? s : 0x7fff;
+        pos[m] = (s < N) ? s : 31;     // padding lanes: key 0, never on the diagonal
         step[m] = 0;
         tie[m] = 0u;
+        top[m] = 0u;
     }
 #pragma unroll
     for (int k = 0; k < N; ++k) {
+        // positions whose tree slot (position - k - 1) survives at step k
+        constexpr unsigned kNone = 0u;
+        const unsigned surv = (k + 1 < 32) ? (unsigned)(((unsigned long long)kSurv << (k + 1)) & 0xffffffffull) : kNone;
 #pragma unroll
         for (int m = 0; m < IM; m++) {
             const bool at = (pos[m] == k);
-            unsigned kd;
-            if constexpr (P == 32) {
-                kd = __reduce_max_sync(kFull, at ? key[m][k] : 0u);
-            } else {
-                const int dl = __ffs(group_ballot<P>(at, gbase)) - 1;
-                kd = __shfl_sync(kFull, key[m][k], gbase + dl);
-            }
-            const int slot = pos[m] - k - 1;
-            const bool ok = (slot >= 0) && (pos[m] < N) && (key[m][k] > kd) && (key[m][k] <= 0x7f800000u) &&
-                            ((kSurv >> (slot & 31)) & 1u);
-            const unsigned cand = ok ? key[m][k] : 0u;
-            const unsigned mx = (P == 32) ? __reduce_max_sync(kFull, cand) : group_max<P>(cand);
-            const bool hit = ok && (cand == mx);
+            const bool live = (surv >> pos[m]) & 1u;
+            const unsigned e = at ? (ek[m][k] | 1u) : (live ? ek[m][k] : 0u);
+            const unsigned mx = (P == 32) ? __reduce_max_sync(kFull, e) : group_max<P>(e);
+            top[m] = max(top[m], mx);
+            const bool hit = !at && (e == mx);
             const unsigned tb = group_ballot<P>(hit, gbase);
             tie[m] |= tb & (tb - 1u);
             int wpos;
             if constexpr (P == 32) wpos = (int)__reduce_max_sync(kFull, hit ? (unsigned)pos[m] : 0u);
             else wpos = __shfl_sync(kFull, pos[m], gbase + (tb ? __ffs(tb) - 1 : 0));
-            if (hit || (at && mx == 0u)) step[m] = k;
-            if (hit) pos[m] = k;
-            else if (at && mx != 0u) pos[m] = wpos;
+            if (hit) {
+                pos[m] = k;
+                step[m] = k;
+            } else if (at) {
+                if (mx & 1u) step[m] = k;
+                else pos[m] = wpos;
+            }
         }
     }
 #pragma unroll
     for (int m = 0; m < IM; m++) {
-        if (tie[m] == 0u && s < N) win[m][step[m]] = s;
-        if (__any_sync(kFull, tie[m] != 0u)) replay_tracked<N, P, MODE, SW>(st[m], win[m], s, gbase);
+        const bool bad = (tie[m] != 0u) || (top[m] > kInfCode + 1u);
+        if (!bad && s < N) win[m][step[m]] = s;
+        if (__any_sync(kFull, bad)) replay_tracked<N, P, MODE, SW>(st[m], win[m], s, gbase);
     }
 }
 
