@@ -138,6 +138,26 @@ int mi_inverse_descr_noalloc_f32(float* d_packed, const int64_t* d_offsets, cons
                                  const int32_t* d_flags, int32_t* d_perm, int32_t* d_info, int64_t count,
                                  uint32_t n_mask, uint32_t mode_mask, void* stream);
 
+/*
+ * Newton-Schulz refinement of n = 32 inverses on the tensor cores (no
+ * reference counterpart: the reference computes in FP32 only, with its FP64
+ * switch commented out, verify.hpp:9):  X <- X + X (I - A X), `steps` times
+ * (1..4).  Products are 3xTF32 (TF32 head and FP32 remainder, FP32
+ * accumulation).  d_a, d_x: batch row-major 32 x 32 FP32 matrices, 16-byte
+ * aligned; d_x is refined in place, d_a is only read.
+ */
+int mi_newton_schulz_f32(const float* d_a, float* d_x, int64_t batch, int n, int steps, void* stream);
+
+/*
+ * One refinement step in FP64 for the matrices listed in d_list[0 .. count)
+ * (indices into a batch of `batch` n x n FP32 matrices, n <= 32): R = I - A X
+ * and X <- X + X R evaluated in FP64, X rounded once to FP32.  For the
+ * matrices a cheap test flags as ill-conditioned, where an FP32 residual is
+ * no better than the inverse itself.  Out-of-range list entries are skipped.
+ */
+int mi_refine_fp64_f32(const float* d_a, float* d_x, const int32_t* d_list, int64_t count, int64_t batch, int n,
+                       void* stream);
+
 /* Threads per block used for size n and pivot mode (0 = built-in default). */
 int mi_set_launch_config(int n, int pivot, int threads_per_block);
 int mi_get_launch_config(int n, int pivot, int* threads_per_block);

@@ -62,6 +62,10 @@ def load(path: str | None = None):
     L.mi_inverse_descr_f32.restype = i32
     L.mi_inverse_descr_noalloc_f32.argtypes = [vp, vp, vp, vp, vp, vp, i64, ctypes.c_uint32, ctypes.c_uint32, vp]
     L.mi_inverse_descr_noalloc_f32.restype = i32
+    L.mi_newton_schulz_f32.argtypes = [vp, vp, i64, i32, i32, vp]
+    L.mi_newton_schulz_f32.restype = i32
+    L.mi_refine_fp64_f32.argtypes = [vp, vp, vp, i64, i64, i32, vp]
+    L.mi_refine_fp64_f32.restype = i32
     L.mi_descr_workspace_bytes.argtypes = [i64]
     L.mi_descr_workspace_bytes.restype = ctypes.c_size_t
     L.mi_set_launch_config.argtypes = [i32, i32, i32]
@@ -93,6 +97,8 @@ def exported_symbols() -> list[str]:
         "mi_inverse_descr_f32",
         "mi_descr_workspace_bytes",
         "mi_inverse_descr_noalloc_f32",
+        "mi_newton_schulz_f32",
+        "mi_refine_fp64_f32",
         "mi_set_launch_config",
         "mi_get_launch_config",
     ]

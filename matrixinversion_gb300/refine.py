@@ -1,0 +1,165 @@
+"""Precision study: FP32 inverses of conditioned 32 x 32 matrices, plain and
+refined by Newton-Schulz steps on the tensor cores.
+
+Matrices are A = Q1 diag(s) Q2^T with Q1, Q2 from QR of seeded Gaussian
+matrices and singular values log-spaced from 1 down to 1/kappa, in buckets of
+kappa (default 1e1, 1e3, 1e5, 1e6).  The reference inverse is FP64 (batched
+LU in FP64 on the device, of the FP32 matrix as stored).  Error of one matrix
+= max |X - X64| / max |X64|.
+
+    python -m matrixinversion_gb300.refine --per-bucket 65536
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import sys
+
+import numpy as np
+
+from . import _lib
+
+KAPPAS = (1e1, 1e3, 1e5, 1e6)
+
+
+def newton_schulz_(A, X, steps: int = 1, stream=None):
+    """Refine X (in place) toward A^-1: X <- X + X (I - A X), `steps` times.
+    A, X: contiguous CUDA float32 [batch, 32, 32]."""
+    import torch
+
+    for name, t in (("A", A), ("X", X)):
+        if not (isinstance(t, torch.Tensor) and t.is_cuda and t.dtype == torch.float32 and t.is_contiguous()):
+            raise TypeError(f"{name} must be a contiguous CUDA float32 tensor")
+    if A.shape != X.shape or A.dim() != 3 or A.shape[-1] != 32 or A.shape[-2] != 32:
+        raise ValueError("A and X must both be [batch, 32, 32]")
+    st = (stream or torch.cuda.current_stream(A.device)).cuda_stream
+    with torch.cuda.device(A.device):
+        status = _lib.load().mi_newton_schulz_f32(ctypes.c_void_p(A.data_ptr()), ctypes.c_void_p(X.data_ptr()),
+                                                  A.shape[0], 32, int(steps), ctypes.c_void_p(st))
+    _lib.check(status)
+    return X
+
+
+def refine_fp64_(A, X, index, stream=None):
+    """One FP64-residual refinement step for the matrices X[index] (in place).
+    index: CUDA int32 tensor of batch indices."""
+    import torch
+
+    if not (index.is_cuda and index.dtype == torch.int32 and index.is_contiguous()):
+        raise TypeError("index must be a contiguous CUDA int32 tensor")
+    n = A.shape[-1]
+    st = (stream or torch.cuda.current_stream(A.device)).cuda_stream
+    with torch.cuda.device(A.device):
+        status = _lib.load().mi_refine_fp64_f32(ctypes.c_void_p(A.data_ptr()), ctypes.c_void_p(X.data_ptr()),
+                                                ctypes.c_void_p(index.data_ptr()), index.numel(), A.shape[0], n,
+                                                ctypes.c_void_p(st))
+    _lib.check(status)
+    return X
+
+
+def flag_ill_conditioned(A, X, threshold: float = 1e4):
+    """Indices (CUDA int32) of matrices whose estimate ||A||_inf ||X||_inf of
+    the condition number is at least `threshold`: there an FP32 residual is
+    no better than the FP32 inverse, and the FP64 step is worth its cost."""
+    import torch
+
+    est = A.abs().sum(-1).amax(-1) * X.abs().sum(-1).amax(-1)
+    est = torch.where(torch.isfinite(est), est, torch.full_like(est, float("inf")))
+    return torch.nonzero(est >= threshold).squeeze(1).to(torch.int32).contiguous()
+
+
+def conditioned(batch: int, kappa: float, n: int = 32, seed: int = 0, device="cuda"):
+    """FP32 [batch, n, n] with 2-norm condition number ~kappa (as FP64)."""
+    import torch
+
+    g = torch.Generator(device=device).manual_seed(seed)
+    G1 = torch.randn(batch, n, n, generator=g, device=device, dtype=torch.float64)
+    G2 = torch.randn(batch, n, n, generator=g, device=device, dtype=torch.float64)
+    Q1, _ = torch.linalg.qr(G1)
+    Q2, _ = torch.linalg.qr(G2)
+    s = torch.logspace(0.0, -float(np.log10(kappa)), n, device=device, dtype=torch.float64)
+    A = (Q1 * s) @ Q2.transpose(1, 2)
+    return A.float().contiguous()
+
+
+def rel_error(X, X64):
+    """Per matrix: max |X - X64| / max |X64|."""
+    d = (X.double() - X64).abs().amax((-1, -2))
+    return d / X64.abs().amax((-1, -2))
+
+
+def study(per_bucket: int = 65536, kappas=KAPPAS, steps=(1, 2), seed: int = 0, timing_iters: int = 5):
+    import torch
+
+    import matrixinversion_gb300 as mi
+
+    out = []
+    for bi, kappa in enumerate(kappas):
+        A = conditioned(per_bucket, kappa, seed=seed + bi)
+        X64 = torch.linalg.inv(A.double())
+        X0, _, info = mi.batched_inverse(A, "partial")
+        row = {"kappa": kappa, "matrices": per_bucket}
+        e0 = rel_error(X0, X64)
+        row["plain"] = {"median": float(e0.median()), "max": float(e0.max())}
+        for k in steps:
+            X = X0.clone()
+            newton_schulz_(A, X, steps=k)
+            e = rel_error(X, X64)
+            row[f"ns{k}"] = {"median": float(e.median()), "max": float(e.max())}
+        # NS step, then the FP64 step for the flagged matrices only
+        X = X0.clone()
+        newton_schulz_(A, X, steps=1)
+        idx = flag_ill_conditioned(A, X)
+        refine_fp64_(A, X, idx)
+        e = rel_error(X, X64)
+        row["ns1_fp64_flagged"] = {"median": float(e.median()), "max": float(e.max()), "flagged": int(idx.numel())}
+        # the reference pivot rule's inverse, plain and after one NS step
+        Xr, _, _ = mi.batched_inverse(A, "reference")
+        e = rel_error(Xr, X64)
+        row["reference_plain"] = {"median": float(e.median()), "max": float(e.max())}
+        newton_schulz_(A, Xr, steps=1)
+        e = rel_error(Xr, X64)
+        row["reference_ns1"] = {"median": float(e.median()), "max": float(e.max())}
+        out.append(row)
+    # throughput on one bucket's batch (kernel time, CUDA events, in place on a copy)
+    A = conditioned(per_bucket, kappas[0], seed=seed)
+    X0, _, _ = mi.batched_inverse(A, "partial")
+    all_idx = torch.arange(per_bucket, dtype=torch.int32, device=A.device)
+    timing = {}
+    for label, fn in (("inverse_partial", lambda X: mi.batched_inverse_(X, "partial")),
+                      ("inverse_reference", lambda X: mi.batched_inverse_(X, "reference")),
+                      ("ns1", lambda X: newton_schulz_(A, X, 1)), ("ns2", lambda X: newton_schulz_(A, X, 2)),
+                      ("fp64_all", lambda X: refine_fp64_(A, X, all_idx))):
+        bufs = [(A if label.startswith("inverse") else X0).clone() for _ in range(timing_iters + 2)]
+        for b in bufs[:2]:
+            fn(b)
+        torch.cuda.synchronize()
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        ev[0].record()
+        for b in bufs[2:]:
+            fn(b)
+        ev[1].record()
+        torch.cuda.synchronize()
+        ms = ev[0].elapsed_time(ev[1]) / timing_iters
+        timing[label] = {"ms": ms, "matrices_per_s": per_bucket / ms * 1e3}
+    out.append({"timing": timing, "matrices": per_bucket})
+    return out
+
+
+def main(argv=None):
+    p = argparse.ArgumentParser()
+    p.add_argument("--per-bucket", type=int, default=65536)
+    p.add_argument("--seed", type=int, default=0)
+    p.add_argument("--out", default=None)
+    a = p.parse_args(argv)
+    rows = study(a.per_bucket, seed=a.seed)
+    for r in rows:
+        print(json.dumps(r), flush=True)
+    if a.out:
+        with open(a.out, "w") as f:
+            json.dump(rows, f, indent=1)
+
+
+if __name__ == "__main__":
+    main(sys.argv[1:])
