@@ -158,7 +158,11 @@ int mi_newton_schulz_f32(const float* d_a, float* d_x, int64_t batch, int n, int
 int mi_refine_fp64_f32(const float* d_a, float* d_x, const int32_t* d_list, int64_t count, int64_t batch, int n,
                        void* stream);
 
-/* Threads per block used for size n and pivot mode (0 = built-in default). */
+/*
+ * Threads per block used for size n and pivot mode whenever a call passes
+ * threads_per_block = 0.  Ships with a table measured on GB300; set 0 to
+ * restore that table's entry.
+ */
 int mi_set_launch_config(int n, int pivot, int threads_per_block);
 int mi_get_launch_config(int n, int pivot, int* threads_per_block);
 

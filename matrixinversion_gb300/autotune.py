@@ -1,0 +1,110 @@
+"""Launch autotuner for the reference's NUMTHREADS knob.
+
+For each (n, pivot mode) it times the kernel at every candidate
+threads-per-block value (matrices per block = threads / lanes per matrix,
+lanes per matrix from mi_query_config) on a seeded uniform batch, each launch
+on a fresh copy of the batch, and installs the fastest with
+mi_set_launch_config.  Both entry points use the installed value whenever the
+caller passes threads_per_block = 0: the contiguous call and every bucket of
+a descriptor call.  Tables can be saved and loaded as JSON.
+
+    python -m matrixinversion_gb300.autotune --n 2-32 --modes none,reference --out tuned.json
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import sys
+
+from . import _lib
+
+CANDIDATES = (32, 64, 96, 128, 160, 192, 224, 256)
+
+
+def _time_one(n: int, mode: str, tpb: int, src, work, iters: int) -> float:
+    import torch
+
+    import matrixinversion_gb300 as mi
+
+    times = []
+    for it in range(iters + 1):
+        work.copy_(src)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        mi.batched_inverse_(work, mode, threads_per_block=tpb)
+        e1.record()
+        torch.cuda.synchronize()
+        if it > 0:
+            times.append(e0.elapsed_time(e1))
+    times.sort()
+    return times[len(times) // 2]
+
+
+def tune(ns=range(1, 33), modes=("none", "reference"), batch: int = 262144, iters: int = 5,
+         candidates=CANDIDATES, install: bool = True, seed: int = 0) -> dict:
+    """{(n, mode): {"best": tpb, "ms": {tpb: ms}}}; installs the best values."""
+    import torch
+
+    table = {}
+    g = torch.Generator(device="cuda").manual_seed(seed)
+    for n in ns:
+        src = torch.rand(batch, n, n, generator=g, device="cuda") * 2 - 1
+        work = torch.empty_like(src)
+        for mode in modes:
+            s = src + n * torch.eye(n, device="cuda") if mode == "none" else src
+            ms = {tpb: _time_one(n, mode, tpb, s, work, iters) for tpb in candidates}
+            best = min(ms, key=ms.get)
+            table[(n, mode)] = {"best": best, "ms": ms}
+            if install:
+                set_config(n, mode, best)
+        del src, work
+    return table
+
+
+def set_config(n: int, mode: str, threads_per_block: int) -> None:
+    _lib.check(_lib.load().mi_set_launch_config(int(n), _lib.PIVOT_MODES[mode], int(threads_per_block)))
+
+
+def get_config(n: int, mode: str) -> int:
+    v = ctypes.c_int(0)
+    _lib.check(_lib.load().mi_get_launch_config(int(n), _lib.PIVOT_MODES[mode], ctypes.byref(v)))
+    return v.value
+
+
+def save(table: dict, path: str) -> None:
+    with open(path, "w") as f:
+        json.dump([{"n": n, "mode": m, **v, "ms": {str(k): t for k, t in v["ms"].items()}}
+                   for (n, m), v in sorted(table.items())], f, indent=1)
+
+
+def load(path: str, install: bool = True) -> dict:
+    with open(path) as f:
+        rows = json.load(f)
+    table = {(r["n"], r["mode"]): {"best": r["best"], "ms": {int(k): t for k, t in r["ms"].items()}} for r in rows}
+    if install:
+        for (n, m), v in table.items():
+            set_config(n, m, v["best"])
+    return table
+
+
+def main(argv=None):
+    from .sweep import parse_range
+
+    p = argparse.ArgumentParser()
+    p.add_argument("--n", default="2-32")
+    p.add_argument("--modes", default="none,reference")
+    p.add_argument("--batch", type=int, default=262144)
+    p.add_argument("--iters", type=int, default=5)
+    p.add_argument("--out", default=None)
+    a = p.parse_args(argv)
+    table = tune(parse_range(a.n), a.modes.split(","), a.batch, a.iters)
+    for (n, m), v in sorted(table.items()):
+        print(json.dumps({"n": n, "mode": m, "best": v["best"], "ms_best": round(v["ms"][v["best"]], 4),
+                          "ms_default": round(v["ms"].get(128, float("nan")), 4)}), flush=True)
+    if a.out:
+        save(table, a.out)
+
+
+if __name__ == "__main__":
+    main(sys.argv[1:])

@@ -21,7 +21,51 @@ static int cuda_fail(cudaError_t e, const char* what) {
 int set_cuda_error(cudaError_t e, const char* what) { return cuda_fail(e, what); }
 
 // Threads per block per (n, pivot mode): 0 = the default; set by the autotuner.
-static int g_tuned[33][4] = {};
+// Threads per block per (n, pivot mode), measured on GB300 by the autotuner
+// (matrixinversion_gb300/autotune.py: 262,144 uniform matrices per size, the
+// fastest of 32..256; reference_serial uses the reference column); 0 = the
+// built-in default of 128.  mi_set_launch_config overrides entries at run
+// time (0 restores this table's entry).
+static const int kTunedGB300[33][4] = {
+    {0, 0, 0, 0},
+    {0, 0, 0, 0},
+    {128, 128, 128, 256},
+    {160, 64, 64, 64},
+    {160, 128, 128, 64},
+    {128, 256, 256, 256},
+    {64, 256, 256, 256},
+    {256, 256, 256, 256},
+    {128, 32, 32, 256},
+    {128, 256, 256, 256},
+    {32, 256, 256, 256},
+    {32, 256, 256, 256},
+    {32, 256, 256, 256},
+    {32, 256, 256, 256},
+    {32, 256, 256, 256},
+    {64, 256, 256, 256},
+    {256, 32, 32, 256},
+    {32, 256, 256, 256},
+    {128, 256, 256, 256},
+    {256, 256, 256, 256},
+    {32, 256, 256, 256},
+    {256, 256, 256, 256},
+    {256, 256, 256, 256},
+    {256, 256, 256, 256},
+    {256, 256, 256, 256},
+    {128, 256, 256, 256},
+    {32, 256, 256, 256},
+    {128, 256, 256, 256},
+    {256, 256, 256, 256},
+    {128, 256, 256, 256},
+    {64, 256, 256, 256},
+    {64, 64, 64, 256},
+    {128, 128, 128, 256}};
+static int g_tuned[33][4];
+static bool g_tuned_init = [] {
+    for (int n = 0; n < 33; n++)
+        for (int m = 0; m < 4; m++) g_tuned[n][m] = kTunedGB300[n][m];
+    return true;
+}();
 
 int tuned_threads(int n, int mode) {
     const int t = (n >= 1 && n <= 32 && mode >= 0 && mode < 4) ? g_tuned[n][mode] : 0;
@@ -137,7 +181,7 @@ int mi_set_launch_config(int n, int pivot, int threads_per_block) {
     if (n < 1 || n > 32 || pivot < 0 || pivot > 3 || threads_per_block < 0 || threads_per_block > 256 ||
         threads_per_block % 32 != 0)
         return MI_ERR_INVALID_VALUE;
-    mi::g_tuned[n][pivot] = threads_per_block;
+    mi::g_tuned[n][pivot] = threads_per_block ? threads_per_block : mi::kTunedGB300[n][pivot];
     return MI_OK;
 }
 

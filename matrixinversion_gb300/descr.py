@@ -123,4 +123,117 @@ class DescrGraph:
         self.graph.replay()
 
 
-__all__ = ["pack", "unpack", "workspace_bytes", "masks", "batched_inverse_descr_", "DescrGraph", "pivot_mode"]
+def uneven_batch(count: int, align: int = 4, seed: int = 0, pivot_flag: int = 1, device="cuda"):
+    """The uneven workload: n ~ U{2..32} (seeded), a 50/50 flag between no
+    pivoting and `pivot_flag`, entries uniform [-1, 1), +n on the diagonal of
+    the no-pivot matrices; packed with `align`-float alignment.  Returns device
+    tensors (packed, offsets, ns, flags)."""
+    import torch
+
+    g = torch.Generator(device="cpu").manual_seed(seed)
+    ns = torch.randint(2, 33, (count,), generator=g, dtype=torch.int32)
+    flags = torch.where(torch.rand(count, generator=g) < 0.5, 0, pivot_flag).to(torch.int32)
+    sz = (ns.long() * ns.long() + align - 1) // align * align
+    offsets = torch.cumsum(sz, 0) - sz
+    total = int(sz.sum())
+    gd = torch.Generator(device=device).manual_seed(seed + 1)
+    packed = torch.rand(total, generator=gd, device=device) * 2 - 1
+    offsets, ns, flags = offsets.to(device), ns.to(device), flags.to(device)
+    sel = (flags == 0).nonzero().squeeze(1)
+    nn_ = ns[sel].long()
+    rep = torch.repeat_interleave(sel, nn_)
+    k = torch.arange(rep.numel(), device=device) - torch.repeat_interleave(torch.cumsum(nn_, 0) - nn_, nn_)
+    packed[offsets[rep] + k * (ns[rep].long() + 1)] += ns[rep].float()
+    return packed, offsets, ns, flags
+
+
+def bench_uneven(count: int = 1_000_000, align: int = 4, iters: int = 10, seed: int = 0, pivot_flag: int = 1):
+    """Descriptor call (eager and graph-captured) vs one contiguous launch per
+    (n, flag) bucket over the same matrices pre-sorted; kernel time by CUDA
+    events, each run on a fresh copy of the inputs."""
+    import torch
+
+    import matrixinversion_gb300 as mi
+
+    packed, offsets, ns, flags = uneven_batch(count, align, seed, pivot_flag)
+    src = packed.clone()
+    ws = torch.empty(max(workspace_bytes(count), 256), dtype=torch.uint8, device=packed.device)
+    info = torch.empty(count, dtype=torch.int32, device=packed.device)
+    n_mask, mode_mask = masks(ns.cpu().numpy(), flags.cpu().numpy())
+
+    def timed(fn, reset):
+        for _ in range(3):
+            reset()
+            fn()
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(iters):
+            reset()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            fn()
+            e1.record()
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        return float(np.median(ts))
+
+    reset = lambda: packed.copy_(src)
+    eager = lambda: batched_inverse_descr_(packed, offsets, ns, flags, info=info, workspace=ws, n_mask=n_mask,
+                                           mode_mask=mode_mask)
+    t_eager = timed(eager, reset)
+    graph = DescrGraph(packed, offsets, ns, flags, info=info, n_mask=n_mask, mode_mask=mode_mask)
+    t_graph = timed(graph.replay, reset)
+    # per-bucket baseline: the same matrices sorted into contiguous buckets
+    host = src.cpu().numpy()
+    nh, fh, oh = ns.cpu().numpy(), flags.cpu().numpy(), offsets.cpu().numpy()
+    buckets = []
+    for n in range(2, 33):
+        for f in np.unique(fh):
+            sel = np.nonzero((nh == n) & (fh == f))[0]
+            if len(sel):
+                idx = (oh[sel][:, None] + np.arange(n * n)[None]).reshape(-1)
+                B = torch.from_numpy(host[idx].reshape(len(sel), n, n)).to(packed.device)
+                buckets.append((int(f), B, B.clone()))
+    names = {0: "none", 1: "reference", 2: "reference_serial", 3: "partial"}
+
+    def per_bucket():
+        for f, B, _ in buckets:
+            mi.batched_inverse_(B, names[f])
+
+    def breset():
+        for _, B, S in buckets:
+            B.copy_(S)
+
+    t_bucket = timed(per_bucket, breset)
+    bytes_alg = float((8 * ns.double() ** 2 + 4 * ns.double() + 4).sum() + 16 * count)
+    return {"count": count, "align": align, "eager_ms": t_eager, "graph_ms": t_graph, "per_bucket_ms": t_bucket,
+            "buckets": len(buckets), "matrices_per_s_graph": count / t_graph * 1e3,
+            "bytes_per_launch": bytes_alg, "GBs_graph": bytes_alg / t_graph / 1e6,
+            "singular": int((info != 0).sum().item())}
+
+
+def main(argv=None):
+    import argparse
+    import json
+
+    p = argparse.ArgumentParser()
+    p.add_argument("--count", type=int, default=1_000_000)
+    p.add_argument("--align", default="4,1")
+    p.add_argument("--tune", action="store_true", help="autotune threads per block first")
+    p.add_argument("--iters", type=int, default=10)
+    a = p.parse_args(argv)
+    if a.tune:
+        from . import autotune
+
+        autotune.tune(range(2, 33), ("none", "reference"), batch=131072, iters=3)
+    for al in a.align.split(","):
+        print(json.dumps({"tuned": a.tune, **bench_uneven(a.count, int(al), a.iters)}), flush=True)
+
+
+__all__ = ["pack", "unpack", "workspace_bytes", "masks", "batched_inverse_descr_", "DescrGraph", "pivot_mode",
+           "uneven_batch", "bench_uneven"]
+
+if __name__ == "__main__":
+    import sys
+
+    main(sys.argv[1:])
