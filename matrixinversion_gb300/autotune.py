@@ -31,6 +31,7 @@ def _time_one(n: int, mode: str, tpb: int, src, work, iters: int) -> float:
     for it in range(iters + 1):
         work.copy_(src)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda._sleep(200_000)       # the host issues the launch while the device waits
         e0.record()
         mi.batched_inverse_(work, mode, threads_per_block=tpb)
         e1.record()

@@ -99,6 +99,12 @@ PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
 
 template <int N>
 static void geom_of(int& lanes, int& mpw, int& smem_warp) {
+    if constexpr (N <= kTinyMax) {     // one thread per matrix, no shared memory
+        lanes = 1;
+        mpw = 32;
+        smem_warp = 0;
+        return;
+    }
     constexpr int L = default_lanes(N, kModeReference);
     lanes = L;
     mpw = Geom<N, L>::M;

@@ -21,6 +21,12 @@ constexpr int kDefaultThreadsPerBlock = 128;
 int device_sm_count();                                  // cached per device (mi_api.cu)
 PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder();  // driver entry point (mi_api.cu)
 
+}  // namespace mi
+
+#include "mi_tiny.cuh"
+
+namespace mi {
+
 // 3-D tensor map over the batch: {column, row, matrix}, box of one warp's
 // group of matrices; the 128-byte swizzle for n = 32 (rows are 128 bytes).
 inline bool make_tensor_map(CUtensorMap* map, float* a, int n, long long batch, int box_rows, int box_matrices) {
@@ -40,6 +46,7 @@ inline bool make_tensor_map(CUtensorMap* map, float* a, int n, long long batch, 
 template <int N, int MODE>
 cudaError_t launch(float* a, int32_t* perm, int32_t* info, long long batch, int tpb, int grid,
                    cudaStream_t stream) {
+    if constexpr (N <= kTinyMax) return launch_tiny<N, MODE>(a, perm, info, batch, tpb, grid, stream);
     constexpr int L = default_lanes(N, MODE);
     using G = Geom<N, L>;
     const int warps = tpb / 32;
@@ -97,6 +104,8 @@ using ilaunch_fn = cudaError_t (*)(float*, const long long*, const int*, const l
 template <int N, int MODE>
 cudaError_t launch_indexed(float* base, const long long* offsets, const int* list, const long long* range,
                            int32_t* perm, int32_t* info, int tpb, int grid, cudaStream_t stream) {
+    if constexpr (N <= kTinyMax)
+        return launch_tiny_indexed<N, MODE>(base, offsets, list, range, perm, info, tpb, grid, stream);
     constexpr int L = default_lanes(N, MODE);
     const int warps = tpb / 32;
     const size_t smem = smem_bytes<N, L, MODE>(warps);

@@ -1,0 +1,314 @@
+// mi_tiny.cuh -- n <= 4: one thread per matrix.
+//
+// At these sizes a matrix is 4 to 64 bytes, and the lane groups of the
+// sub-warp kernel spend more instructions on coordination than on the
+// arithmetic.  Here each thread loads its matrix into registers, evaluates
+// the pivot rule serially (the reference's tree with T = n slots, the
+// serial scan, or partial pivoting on the updated column) and runs the same
+// Gauss-Jordan step as gj_step / gj_step_partial, element for element:
+// m = c * (1/pivot), a = fma(-m, w, a) with column k zeroed first and w[k] = 1,
+// the pivot row updated with c = 0, rows scaled by 1/pivot at the end.  So
+// results are the sub-warp kernel's, bit for bit.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "mi_kernel.cuh"
+
+namespace mi {
+
+constexpr int kTinyMax = 4;
+
+// |x| with subnormals flushed to zero, NaN kept (compares as false): the
+// reference's fast-math fabs in its pivot compares.
+__device__ __forceinline__ float tiny_ref_key(float x) {
+    const float a = fabsf(x);
+    return (a < 1.17549435e-38f) ? 0.0f : a;
+}
+
+template <int N>
+__device__ __forceinline__ float tiny_get(const float (&a)[N][N], int r, int c) {
+    float v = a[0][c];
+#pragma unroll
+    for (int i = 1; i < N; i++)
+        if (r == i) v = a[i][c];
+    return v;
+}
+
+// Pivot sequence of the reference rules on the raw matrix: win[k] = input
+// row placed at step k.  Parallel rule: per slot t, the diagonal against row
+// k+1+t (strict '>'), then the tree with strides T/2 .. 1 (strict '<').
+template <int N, int MODE>
+__device__ __forceinline__ void tiny_pivots(const float (&a)[N][N], int (&win)[N]) {
+#pragma unroll
+    for (int i = 0; i < N; i++) win[i] = i;
+#pragma unroll
+    for (int k = 0; k < N; k++) {
+        int p = k;
+        if constexpr (MODE == kModeReference) {
+            float vals[N];
+            int idxs[N];
+            const float dk = tiny_ref_key(tiny_get<N>(a, win[k], k));
+#pragma unroll
+            for (int t = 0; t < N; t++) {
+                vals[t] = dk;
+                idxs[t] = k;
+                const int i = k + 1 + t;
+                if (i < N) {
+                    const float w = tiny_ref_key(tiny_get<N>(a, win[i], k));
+                    if (w > vals[t]) {
+                        vals[t] = w;
+                        idxs[t] = i;
+                    }
+                }
+            }
+#pragma unroll
+            for (int s = N / 2; s > 0; s >>= 1)
+#pragma unroll
+                for (int t = 0; t < s; t++)
+                    if (vals[t] < vals[t + s]) {
+                        vals[t] = vals[t + s];
+                        idxs[t] = idxs[t + s];
+                    }
+            p = idxs[0];
+        } else {   // serial scan
+            float mv = tiny_ref_key(tiny_get<N>(a, win[k], k));
+#pragma unroll
+            for (int i = k + 1; i < N; i++) {
+                const float w = tiny_ref_key(tiny_get<N>(a, win[i], k));
+                if (w > mv) {
+                    mv = w;
+                    p = i;
+                }
+            }
+        }
+        // swap win[k] and win[p] (p >= k, runtime)
+        const int wk = win[k];
+        int wp = win[k];
+#pragma unroll
+        for (int i = k + 1; i < N; i++)
+            if (p == i) wp = win[i];
+#pragma unroll
+        for (int i = k + 1; i < N; i++)
+            if (p == i) win[i] = wk;
+        win[k] = wp;
+    }
+}
+
+// One Gauss-Jordan step on rows already in pivot order (as gj_step).
+template <int N>
+__device__ __forceinline__ void tiny_step(float (&b)[N][N], float (&ps)[N], float (&dv)[N], const int k) {
+    float c[N], w[N];
+#pragma unroll
+    for (int i = 0; i < N; i++) c[i] = b[i][k];
+#pragma unroll
+    for (int j = 0; j < N; j++) w[j] = b[k][j];
+    const float d = b[k][k];
+    const float p = recip(d);
+    dv[k] = d;
+    ps[k] = p;
+    c[k] = 0.0f;
+    w[k] = 1.0f;
+#pragma unroll
+    for (int i = 0; i < N; i++) b[i][k] = 0.0f;
+    b[k][k] = 1.0f;
+#pragma unroll
+    for (int i = 0; i < N; i++) {
+        const float m = c[i] * p;
+#pragma unroll
+        for (int j = 0; j < N; j++) b[i][j] = fmaf(-m, w[j], b[i][j]);
+    }
+}
+
+// Partial pivoting step (as gj_step_partial): argmax of |column k| over rows
+// k.. (first maximum; a NaN never beats a number), rows k and r exchanged,
+// then the step.  ra[s] = input row at logical row s.
+template <int N>
+__device__ __forceinline__ void tiny_step_partial(float (&b)[N][N], float (&ps)[N], float (&dv)[N], int (&ra)[N],
+                                                  const int k) {
+    unsigned best = 0u;
+    int r = k;
+#pragma unroll
+    for (int s = k; s < N; s++) {
+        const unsigned bits = __float_as_uint(b[s][k]) & 0x7fffffffu;
+        const unsigned key = (bits > 0x7f800000u) ? 1u : bits + 2u;
+        if (key > best) {
+            best = key;
+            r = s;
+        }
+    }
+#pragma unroll
+    for (int s = k + 1; s < N; s++) {
+        if (r == s) {
+#pragma unroll
+            for (int j = 0; j < N; j++) {
+                const float t = b[k][j];
+                b[k][j] = b[s][j];
+                b[s][j] = t;
+            }
+            const int t = ra[k];
+            ra[k] = ra[s];
+            ra[s] = t;
+        }
+    }
+    tiny_step<N>(b, ps, dv, k);
+}
+
+// Invert one matrix in registers.  a: rows as loaded; on return b holds the
+// scaled inverse of the pivot-ordered matrix, win the pivot order, info the
+// first exactly-zero pivot (1-based) or 0.
+template <int N, int MODE>
+__device__ __forceinline__ void tiny_invert(const float (&a)[N][N], float (&b)[N][N], int (&win)[N], int& info) {
+    if constexpr (MODE == kModeReference || MODE == kModeReferenceSerial) {
+        tiny_pivots<N, MODE>(a, win);
+#pragma unroll
+        for (int i = 0; i < N; i++)
+#pragma unroll
+            for (int j = 0; j < N; j++) b[i][j] = tiny_get<N>(a, win[i], j);
+    } else {
+#pragma unroll
+        for (int i = 0; i < N; i++) {
+            win[i] = i;
+#pragma unroll
+            for (int j = 0; j < N; j++) b[i][j] = a[i][j];
+        }
+    }
+    float ps[N], dv[N];
+#pragma unroll
+    for (int k = 0; k < N; k++) {
+        if constexpr (MODE == kModePartial) tiny_step_partial<N>(b, ps, dv, win, k);
+        else tiny_step<N>(b, ps, dv, k);
+    }
+#pragma unroll
+    for (int i = 0; i < N; i++)
+#pragma unroll
+        for (int j = 0; j < N; j++) b[i][j] = b[i][j] * ps[i];
+    info = 0;
+#pragma unroll
+    for (int k = N - 1; k >= 0; k--)
+        if (dv[k] == 0.0f) info = k + 1;
+}
+
+template <int N>
+__device__ __forceinline__ void tiny_load(const float* src, float (&a)[N][N]) {
+    if constexpr (N == 4 || N == 2) {
+        // 16-byte aligned when the batch is (the launcher checks)
+        const float4* s4 = reinterpret_cast<const float4*>(src);
+#pragma unroll
+        for (int q = 0; q < N * N / 4; q++) {
+            const float4 v = s4[q];
+            const float t[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+            for (int e = 0; e < 4; e++) a[(4 * q + e) / N][(4 * q + e) % N] = t[e];
+        }
+    } else {
+#pragma unroll
+        for (int e = 0; e < N * N; e++) a[e / N][e % N] = src[e];
+    }
+}
+
+// Store with the column permutation A^-1[i][win[j]] = b[i][j].
+template <int N>
+__device__ __forceinline__ void tiny_store(float* dst, const float (&b)[N][N], const int (&win)[N], bool vec) {
+    float o[N][N];
+#pragma unroll
+    for (int i = 0; i < N; i++)
+#pragma unroll
+        for (int c = 0; c < N; c++) {
+            float v = b[i][0];
+#pragma unroll
+            for (int j = 1; j < N; j++)
+                if (win[j] == c) v = b[i][j];
+            o[i][c] = v;
+        }
+    if constexpr (N == 4 || N == 2) {
+        if (vec) {
+            float4* d4 = reinterpret_cast<float4*>(dst);
+#pragma unroll
+            for (int q = 0; q < N * N / 4; q++) {
+                const int e = 4 * q;
+                d4[q] = make_float4(o[e / N][e % N], o[(e + 1) / N][(e + 1) % N], o[(e + 2) / N][(e + 2) % N],
+                                    o[(e + 3) / N][(e + 3) % N]);
+            }
+            return;
+        }
+    }
+#pragma unroll
+    for (int e = 0; e < N * N; e++) dst[e] = o[e / N][e % N];
+}
+
+template <int N, int MODE>
+__global__ void __launch_bounds__(256) mi_tiny_kernel(float* __restrict__ A, int32_t* __restrict__ perm_out,
+                                                      int32_t* __restrict__ info_out, long long batch, int vec) {
+    for (long long b = (long long)blockIdx.x * blockDim.x + threadIdx.x; b < batch;
+         b += (long long)gridDim.x * blockDim.x) {
+        float a[N][N], x[N][N];
+        float* src = A + b * (N * N);
+        if (vec) tiny_load<N>(src, a);
+        else {
+#pragma unroll
+            for (int e = 0; e < N * N; e++) a[e / N][e % N] = src[e];
+        }
+        int win[N], info;
+        tiny_invert<N, MODE>(a, x, win, info);
+        tiny_store<N>(src, x, win, vec != 0);
+        if (perm_out != nullptr) {
+#pragma unroll
+            for (int i = 0; i < N; i++) perm_out[b * N + i] = win[i];
+        }
+        if (info_out != nullptr) info_out[b] = info;
+    }
+}
+
+// Descriptor bucket: list[range[0] .. range[0] + range[1]) at base + offsets[i].
+template <int N, int MODE>
+__global__ void __launch_bounds__(256) mi_tiny_indexed_kernel(float* __restrict__ base,
+                                                              const long long* __restrict__ offsets,
+                                                              const int* __restrict__ list,
+                                                              const long long* __restrict__ range,
+                                                              int32_t* __restrict__ perm_out,
+                                                              int32_t* __restrict__ info_out) {
+    const long long start = range[0], count = range[1];
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < count;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int idx = list[start + t];
+        float* src = base + offsets[idx];
+        float a[N][N], x[N][N];
+#pragma unroll
+        for (int e = 0; e < N * N; e++) a[e / N][e % N] = src[e];
+        int win[N], info;
+        tiny_invert<N, MODE>(a, x, win, info);
+        tiny_store<N>(src, x, win, false);
+        if (perm_out != nullptr) {
+#pragma unroll
+            for (int i = 0; i < N; i++) perm_out[(long long)idx * 32 + i] = win[i];
+        }
+        if (info_out != nullptr) info_out[idx] = info;
+    }
+}
+
+template <int N, int MODE>
+cudaError_t launch_tiny(float* a, int32_t* perm, int32_t* info, long long batch, int tpb, int grid,
+                        cudaStream_t stream) {
+    const int vec = ((N == 4 || N == 2) && (reinterpret_cast<uintptr_t>(a) & 15u) == 0) ? 1 : 0;
+    if (grid <= 0) {
+        const long long need = (batch + tpb - 1) / tpb;
+        const long long cap = 16LL * device_sm_count();
+        grid = (int)(need < cap ? need : cap);
+    }
+    if (grid < 1) grid = 1;
+    mi_tiny_kernel<N, MODE><<<grid, tpb, 0, stream>>>(a, perm, info, batch, vec);
+    return cudaGetLastError();
+}
+
+template <int N, int MODE>
+cudaError_t launch_tiny_indexed(float* base, const long long* offsets, const int* list, const long long* range,
+                                int32_t* perm, int32_t* info, int tpb, int grid, cudaStream_t stream) {
+    if (grid <= 0) grid = 16 * device_sm_count();
+    mi_tiny_indexed_kernel<N, MODE><<<grid, tpb, 0, stream>>>(base, offsets, list, range, perm, info);
+    return cudaGetLastError();
+}
+
+}  // namespace mi
