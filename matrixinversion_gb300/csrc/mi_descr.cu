@@ -18,14 +18,23 @@ constexpr size_t kOffCursors = 1024;             // unsigned long long[128]
 constexpr size_t kOffRanges = 2048;              // long long[128][2]: start, count
 constexpr size_t kOffList = 4096;                // int32[count]
 
+// Bucket counts: a shared-memory histogram per block, then one global
+// atomic per non-empty bucket per block (a million descriptors land on a few
+// dozen buckets, so per-descriptor global atomics would serialise).
 __global__ void descr_count(const int32_t* __restrict__ ns, const int32_t* __restrict__ flags, long long count,
                             unsigned long long* __restrict__ counts, int32_t* __restrict__ info) {
+    __shared__ unsigned int hist[kBuckets];
+    for (int b = threadIdx.x; b < kBuckets; b += blockDim.x) hist[b] = 0u;
+    __syncthreads();
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < count;
          i += (long long)gridDim.x * blockDim.x) {
         const int n = ns[i], f = flags[i];
-        if (n >= 1 && n <= 32 && f >= 0 && f <= 3) atomicAdd(&counts[(n - 1) * 4 + f], 1ull);
+        if (n >= 1 && n <= 32 && f >= 0 && f <= 3) atomicAdd(&hist[(n - 1) * 4 + f], 1u);
         else if (info != nullptr) info[i] = -1;   // malformed descriptor: reported, not processed
     }
+    __syncthreads();
+    for (int b = threadIdx.x; b < kBuckets; b += blockDim.x)
+        if (hist[b] != 0u) atomicAdd(&counts[b], (unsigned long long)hist[b]);
 }
 
 __global__ void descr_scan(const unsigned long long* __restrict__ counts, unsigned long long* __restrict__ cursors,
@@ -48,15 +57,33 @@ __global__ void descr_scan(const unsigned long long* __restrict__ counts, unsign
     ranges[2 * t + 1] = (long long)counts[t];
 }
 
+// List scatter in chunks of blockDim descriptors: the block ranks each
+// descriptor within its bucket in shared memory, reserves the chunk's range
+// of every bucket with one global atomic, then writes the indices.  (Order
+// within a bucket is not significant: each matrix is independent.)
 __global__ void descr_scatter(const int32_t* __restrict__ ns, const int32_t* __restrict__ flags, long long count,
                               unsigned long long* __restrict__ cursors, int32_t* __restrict__ list) {
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < count;
-         i += (long long)gridDim.x * blockDim.x) {
-        const int n = ns[i], f = flags[i];
-        if (n >= 1 && n <= 32 && f >= 0 && f <= 3) {
-            const unsigned long long p = atomicAdd(&cursors[(n - 1) * 4 + f], 1ull);
-            list[p] = (int32_t)i;
+    __shared__ unsigned int hist[kBuckets];
+    __shared__ unsigned long long base[kBuckets];
+    for (long long c0 = (long long)blockIdx.x * blockDim.x; c0 < count; c0 += (long long)gridDim.x * blockDim.x) {
+        for (int b = threadIdx.x; b < kBuckets; b += blockDim.x) hist[b] = 0u;
+        __syncthreads();
+        const long long i = c0 + threadIdx.x;
+        int bucket = -1;
+        unsigned int rank = 0u;
+        if (i < count) {
+            const int n = ns[i], f = flags[i];
+            if (n >= 1 && n <= 32 && f >= 0 && f <= 3) {
+                bucket = (n - 1) * 4 + f;
+                rank = atomicAdd(&hist[bucket], 1u);
+            }
         }
+        __syncthreads();
+        for (int b = threadIdx.x; b < kBuckets; b += blockDim.x)
+            if (hist[b] != 0u) base[b] = atomicAdd(&cursors[b], (unsigned long long)hist[b]);
+        __syncthreads();
+        if (bucket >= 0) list[base[bucket] + rank] = (int32_t)i;
+        __syncthreads();
     }
 }
 

@@ -1015,6 +1015,25 @@ __device__ __forceinline__ void phase_perm_info(const float* scr0, int lane, lon
     __syncwarp();
 }
 
+// n = 32 stage that arrived row-major (1-D copies) -> the 128-byte swizzle of
+// stage_off, in place: 16-byte chunk c of row r moves to c ^ (r & 7).  Each
+// warp instruction reads and writes 4 whole rows, so neither side conflicts.
+template <int M>
+__device__ __forceinline__ void swizzle_stage32(float* slot, int lane) {
+    constexpr int kPer = M * 32 * 8 / 32;      // 16-byte chunks per lane
+    float4* s4 = reinterpret_cast<float4*>(slot);
+    float4 v[kPer];
+#pragma unroll
+    for (int q = 0; q < kPer; q++) v[q] = s4[q * 32 + lane];
+    __syncwarp();
+#pragma unroll
+    for (int q = 0; q < kPer; q++) {
+        const int e = q * 32 + lane, row = e >> 3, c = e & 7;
+        s4[(row << 3) | (c ^ (row & 7))] = v[q];
+    }
+    __syncwarp();
+}
+
 // Per-warp shared memory carving.
 template <int N, int L, int MODE>
 struct WarpSmem {
@@ -1237,7 +1256,12 @@ __global__ void __launch_bounds__(256, 2) mi_inverse_indexed_kernel(float* __res
         __syncwarp();
 
         float a[R][C];
-        phase_load<N, L, MODE, false>(a, sm.slot, sm.scr0, lane);
+        if constexpr (N == 32) {
+            swizzle_stage32<M>(sm.slot, lane);
+            phase_load<N, L, MODE, true>(a, sm.slot, sm.scr0, lane);
+        } else {
+            phase_load<N, L, MODE, false>(a, sm.slot, sm.scr0, lane);
+        }
 
         long long idx[M];
         float* gout[M];
