@@ -1,6 +1,6 @@
-// mi_tiny.cuh -- n <= 4: one thread per matrix.
+// mi_tiny.cuh -- n <= 8: one thread per matrix.
 //
-// At these sizes a matrix is 4 to 64 bytes, and the lane groups of the
+// At these sizes a matrix is 4 to 256 bytes, and the lane groups of the
 // sub-warp kernel spend more instructions on coordination than on the
 // arithmetic.  Here each thread loads its matrix into registers, evaluates
 // the pivot rule serially (the reference's tree with T = n slots, the
@@ -19,7 +19,7 @@
 
 namespace mi {
 
-constexpr int kTinyMax = 4;
+constexpr int kTinyMax = 8;
 
 // |x| with subnormals flushed to zero, NaN kept (compares as false): the
 // reference's fast-math fabs in its pivot compares.
@@ -139,19 +139,29 @@ __device__ __forceinline__ void tiny_step_partial(float (&b)[N][N], float (&ps)[
             r = s;
         }
     }
+    // exchange rows k and r with selects (r is a runtime value)
 #pragma unroll
-    for (int s = k + 1; s < N; s++) {
-        if (r == s) {
+    for (int j = 0; j < N; j++) {
+        const float bk = b[k][j];
+        float nk = bk;
 #pragma unroll
-            for (int j = 0; j < N; j++) {
-                const float t = b[k][j];
-                b[k][j] = b[s][j];
-                b[s][j] = t;
-            }
-            const int t = ra[k];
-            ra[k] = ra[s];
-            ra[s] = t;
+        for (int s = k + 1; s < N; s++) {
+            const bool hit = (r == s);
+            nk = hit ? b[s][j] : nk;
+            b[s][j] = hit ? bk : b[s][j];
         }
+        b[k][j] = nk;
+    }
+    {
+        const int rk = ra[k];
+        int nk = rk;
+#pragma unroll
+        for (int s = k + 1; s < N; s++) {
+            const bool hit = (r == s);
+            nk = hit ? ra[s] : nk;
+            ra[s] = hit ? rk : ra[s];
+        }
+        ra[k] = nk;
     }
     tiny_step<N>(b, ps, dv, k);
 }
@@ -193,8 +203,8 @@ __device__ __forceinline__ void tiny_invert(const float (&a)[N][N], float (&b)[N
 
 template <int N>
 __device__ __forceinline__ void tiny_load(const float* src, float (&a)[N][N]) {
-    if constexpr (N == 4 || N == 2) {
-        // 16-byte aligned when the batch is (the launcher checks)
+    if constexpr ((N * N) % 4 == 0) {
+        // n * n a multiple of 4: 16-byte aligned whenever the batch is (the launcher checks)
         const float4* s4 = reinterpret_cast<const float4*>(src);
 #pragma unroll
         for (int q = 0; q < N * N / 4; q++) {
@@ -223,7 +233,7 @@ __device__ __forceinline__ void tiny_store(float* dst, const float (&b)[N][N], c
                 if (win[j] == c) v = b[i][j];
             o[i][c] = v;
         }
-    if constexpr (N == 4 || N == 2) {
+    if constexpr ((N * N) % 4 == 0) {
         if (vec) {
             float4* d4 = reinterpret_cast<float4*>(dst);
 #pragma unroll
@@ -239,26 +249,73 @@ __device__ __forceinline__ void tiny_store(float* dst, const float (&b)[N][N], c
     for (int e = 0; e < N * N; e++) dst[e] = o[e / N][e % N];
 }
 
+// Contiguous batch, one matrix per thread.  When n * n is a multiple of 4
+// each thread moves its matrix with 16-byte loads and stores (16-byte-aligned
+// batch); otherwise each warp's 32 consecutive matrices move between global
+// and shared memory with coalesced copies and each thread reads and writes
+// its own matrix there at an odd pitch (conflict-free).  Measured on GB300:
+// the staged copies win for n = 3, 5, 7 and lose for n = 2, 4, 6, 8.
+constexpr int kTinyThreads = 128;
+
+template <int N>
+__host__ __device__ constexpr int tiny_pitch() { return (N * N) | 1; }
+
 template <int N, int MODE>
-__global__ void __launch_bounds__(256) mi_tiny_kernel(float* __restrict__ A, int32_t* __restrict__ perm_out,
-                                                      int32_t* __restrict__ info_out, long long batch, int vec) {
-    for (long long b = (long long)blockIdx.x * blockDim.x + threadIdx.x; b < batch;
-         b += (long long)gridDim.x * blockDim.x) {
+__global__ void __launch_bounds__(kTinyThreads) mi_tiny_kernel(float* __restrict__ A, int32_t* __restrict__ perm_out,
+                                                              int32_t* __restrict__ info_out, long long batch,
+                                                              int vec) {
+    constexpr int NN = N * N, P = tiny_pitch<N>();
+    if constexpr (NN % 4 == 0) {
+        for (long long b = (long long)blockIdx.x * blockDim.x + threadIdx.x; b < batch;
+             b += (long long)gridDim.x * blockDim.x) {
+            float a[N][N], x[N][N];
+            float* src = A + b * NN;
+            if (vec) tiny_load<N>(src, a);
+            else {
+#pragma unroll
+                for (int e = 0; e < NN; e++) a[e / N][e % N] = src[e];
+            }
+            int win[N], info;
+            tiny_invert<N, MODE>(a, x, win, info);
+            tiny_store<N>(src, x, win, vec != 0);
+            if (perm_out != nullptr) {
+#pragma unroll
+                for (int i = 0; i < N; i++) perm_out[b * N + i] = win[i];
+            }
+            if (info_out != nullptr) info_out[b] = info;
+        }
+        return;
+    }
+    __shared__ float stage[kTinyThreads / 32][32 * P];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    float* st = stage[warp];
+    const long long wstride = (long long)gridDim.x * (kTinyThreads / 32) * 32;
+    for (long long b0 = ((long long)blockIdx.x * (kTinyThreads / 32) + warp) * 32; b0 < batch; b0 += wstride) {
+        const int cnt = (batch - b0 < 32) ? (int)(batch - b0) : 32;
+        float* g = A + b0 * NN;
+        for (int e = lane; e < cnt * NN; e += 32) st[(e / NN) * P + (e % NN)] = g[e];
+        __syncwarp();
+        const bool mine = lane < cnt;
         float a[N][N], x[N][N];
-        float* src = A + b * (N * N);
-        if (vec) tiny_load<N>(src, a);
-        else {
+        int win[N], info = 0;
+        if (mine) {
+            float* sm = st + lane * P;
 #pragma unroll
-            for (int e = 0; e < N * N; e++) a[e / N][e % N] = src[e];
+            for (int e = 0; e < NN; e++) a[e / N][e % N] = sm[e];
+            tiny_invert<N, MODE>(a, x, win, info);
+            tiny_store<N>(sm, x, win, false);
         }
-        int win[N], info;
-        tiny_invert<N, MODE>(a, x, win, info);
-        tiny_store<N>(src, x, win, vec != 0);
-        if (perm_out != nullptr) {
+        __syncwarp();
+        for (int e = lane; e < cnt * NN; e += 32) g[e] = st[(e / NN) * P + (e % NN)];
+        if (mine) {
+            const long long b = b0 + lane;
+            if (perm_out != nullptr) {
 #pragma unroll
-            for (int i = 0; i < N; i++) perm_out[b * N + i] = win[i];
+                for (int i = 0; i < N; i++) perm_out[b * N + i] = win[i];
+            }
+            if (info_out != nullptr) info_out[b] = info;
         }
-        if (info_out != nullptr) info_out[b] = info;
+        __syncwarp();
     }
 }
 
@@ -290,16 +347,18 @@ __global__ void __launch_bounds__(256) mi_tiny_indexed_kernel(float* __restrict_
 }
 
 template <int N, int MODE>
-cudaError_t launch_tiny(float* a, int32_t* perm, int32_t* info, long long batch, int tpb, int grid,
+cudaError_t launch_tiny(float* a, int32_t* perm, int32_t* info, long long batch, int /*tpb*/, int grid,
                         cudaStream_t stream) {
-    const int vec = ((N == 4 || N == 2) && (reinterpret_cast<uintptr_t>(a) & 15u) == 0) ? 1 : 0;
+    // the block size is fixed by the static staging buffer
     if (grid <= 0) {
-        const long long need = (batch + tpb - 1) / tpb;
+        const long long per_block = kTinyThreads;      // one matrix per thread
+        const long long need = (batch + per_block - 1) / per_block;
         const long long cap = 16LL * device_sm_count();
         grid = (int)(need < cap ? need : cap);
     }
     if (grid < 1) grid = 1;
-    mi_tiny_kernel<N, MODE><<<grid, tpb, 0, stream>>>(a, perm, info, batch, vec);
+    const int vec = ((N * N) % 4 == 0 && (reinterpret_cast<uintptr_t>(a) & 15u) == 0) ? 1 : 0;
+    mi_tiny_kernel<N, MODE><<<grid, kTinyThreads, 0, stream>>>(a, perm, info, batch, vec);
     return cudaGetLastError();
 }
 
