@@ -72,10 +72,12 @@ __device__ int g_device_error;
 
 __host__ __device__ constexpr int pow2_at_least(int n) { return n <= 4 ? 4 : (n <= 8 ? 8 : (n <= 16 ? 16 : 32)); }
 
-// Lanes per matrix used by default: two matrices per warp for n > 8 keeps
-// 8 x 8 (n = 32) register blocks, i.e. 16 broadcast values per 64 FMAs.
+// Lanes per matrix used by default (n <= 8 runs one thread per matrix):
+// 16 lanes for n > 16 keeps 8 x 8 register blocks (n = 32), i.e. 16 broadcast
+// values per 64 FMAs; 8 lanes for n = 11..16 and 4 for n = 9, 10 (measured on
+// GB300: 4 lanes lose from n = 12 up).
 __host__ __device__ constexpr int default_lanes(int n, int mode) {
-    return mode == kModePartial ? pow2_at_least(n) : (n > 16 ? 16 : (n > 4 ? 8 : 4));
+    return mode == kModePartial ? pow2_at_least(n) : (n > 16 ? 16 : (n > 10 ? 8 : 4));
 }
 
 // ---------------------------------------------------------------------------

@@ -53,7 +53,7 @@ def test_query_and_errors_without_gpu(lib):
     assert lib.mi_abi_version() == 1
     lanes, mpw, smem, tpb = (ctypes.c_int() for _ in range(4))
     # n <= 8: one thread per matrix, no shared memory; larger n: lane groups
-    for n, want in ((1, 1), (4, 1), (5, 1), (8, 1), (9, 8), (16, 8), (17, 16), (32, 16)):
+    for n, want in ((1, 1), (4, 1), (5, 1), (8, 1), (9, 4), (10, 4), (11, 8), (16, 8), (17, 16), (32, 16)):
         assert lib.mi_query_config(n, ctypes.byref(lanes), ctypes.byref(mpw), ctypes.byref(smem),
                                    ctypes.byref(tpb)) == 0
         assert lanes.value == want and mpw.value == 32 // want and (smem.value > 0) == (n > 8)
