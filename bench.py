@@ -217,6 +217,7 @@ def main():
     import matrixinversion_gb300 as mi
     from matrixinversion_gb300 import build as B
     from matrixinversion_gb300 import data
+    from matrixinversion_gb300 import shards
     from matrixinversion_gb300.host import HostPipeline
 
     if rank == 0 or not os.path.exists(B.LIB):
@@ -226,7 +227,7 @@ def main():
     mi._lib.load()
 
     n, batch = args.n, args.batch
-    host = data.uniform(args.seed + 7919 * rank, batch, n)
+    host = data.uniform(shards.shard_seed(args.seed, rank), batch, n)
     if args.pivot == "none":
         host += np.float32(n) * np.eye(n, dtype=np.float32)
     src = torch.from_numpy(host).to(dev)
@@ -259,11 +260,8 @@ def main():
         barrier()
     total_ms = t_start.elapsed_time(t_end)
     launch_ms = [a.elapsed_time(b) for a, b in ev]
-    if world > 1:
-        t = torch.tensor([total_ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = world * batch * args.steps / (total_ms / 1e3)
+    total_ms = shards.max_over_ranks(total_ms, device=dev)
+    value = shards.aggregate_rate(batch * args.steps, total_ms / 1e3, world)
     del bufs
     torch.cuda.empty_cache()
 
@@ -284,11 +282,8 @@ def main():
             pipe.run(hA, args.pivot, hX, hP, hI)
         barrier()
         dt = time.perf_counter() - t0
-        if world > 1:
-            t = torch.tensor([dt], device=dev)
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            dt = float(t.item())
-        e2e = {"value": world * batch * e2e_steps / dt, "unit": UNIT,
+        dt = shards.max_over_ranks(dt, device=dev)
+        e2e = {"value": shards.aggregate_rate(batch * e2e_steps, dt, world), "unit": UNIT,
                "h2d_bytes_per_step": batch * n * n * 4,
                "d2h_bytes_per_step": batch * n * n * 4 + batch * n * 4 + batch * 4,
                "steps": e2e_steps, "chunk_matrices": 65536, "streams": 3}
