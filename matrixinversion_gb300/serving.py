@@ -10,8 +10,9 @@ them first come, first served into a device pool with a fixed HBM budget:
   half, so a half is the largest batch and the budget bounds what is resident;
 * one batch = one host-to-device copy of its contiguous span of the ring, one
   descriptor call (GPU bucketing by size, one persistent launch per size
-  present) and one device-to-host copy into the output ring, on separate
-  copy and compute streams so that consecutive batches overlap;
+  present; a batch of one size stored back to back takes a single contiguous
+  launch instead) and one device-to-host copy into the output ring, on
+  separate copy and compute streams so that consecutive batches overlap;
 * a request completes when the host sees its batch's last copy finish.
 
 The baseline ("per_request") runs the same loop with one request per batch
@@ -182,7 +183,15 @@ class CudaServer:
         m0 = int(self.mat_first[i])
         m1 = int(self.mat_first[j - 1] + t.k[j - 1])
         with torch.cuda.stream(self.s_cmp):
-            if coalesce:
+            nb = t.n[i:j]
+            packed = bool(np.all(t.offset[i + 1:j] == t.offset[i:j - 1] + t.floats[i:j - 1]))
+            if coalesce and nb.min() == nb.max() and packed:
+                # one size, back to back in the ring: a single contiguous launch
+                status = self.L.mi_inverse_f32(ctypes.c_void_p(dst.data_ptr()), None,
+                                               ctypes.c_void_p(self.d_info[m0:m1].data_ptr()), m1 - m0, int(nb[0]),
+                                               self.pivot, st)
+                self.check(status)
+            elif coalesce:
                 offs = torch.sub(self.d_off[m0:m1], base, out=self.d_rel[m0:m1])
                 status = self.L.mi_inverse_descr_f32(
                     ctypes.c_void_p(dst.data_ptr()), ctypes.c_void_p(offs.data_ptr()),
