@@ -417,12 +417,15 @@ __device__ __noinline__ void replay_tracked(const float* st, int* win, int s, in
 
 // The tracked replay for IM matrices at once (independent chains that
 // overlap).  Keys are encoded 2|x| for a candidate and 2|x| + 1 for the row on
-// the diagonal, so one group maximum decides the step: an odd maximum means
-// no surviving candidate beats the diagonal strictly (it stays), an even one
-// names the winner.  A second maximum brings the winner's position to the
-// row it displaces.  Lanes record the step at which they are placed.  Ties
-// between candidates and NaNs that take part (codes above 2 * inf + 1) are
-// only flagged here; such a matrix is replayed again by replay_tracked.
+// the diagonal (|x| from fast_key: subnormals 0, NaN above every number), so
+// one group maximum decides the step: an odd maximum means no surviving
+// candidate beats the diagonal strictly (it stays), an even one names the
+// winner.  A second maximum brings the winner's old position to the row it
+// displaces.  A placed row never moves again, so its final position is the
+// step that placed it; a tie between candidates leaves two rows at one
+// position, found by one match after the last step.  Such a matrix, or one
+// where a NaN competed (codes above 2 * inf + 1), is replayed again by
+// replay_tracked with the exact keys and the tree's tie order.
 template <int N, int P, int IM, int MODE, bool SW = (N == 32)>
 __device__ __forceinline__ void replay_tracked_multi(const float* const (&st)[IM], int* const (&win)[IM], int s,
                                                      int gbase) {
@@ -432,21 +435,18 @@ __device__ __forceinline__ void replay_tracked_multi(const float* const (&st)[IM
 #pragma unroll
     for (int m = 0; m < IM; m++)
 #pragma unroll
-        for (int k = 0; k < N; k++) ek[m][k] = (s < N) ? (pivot_key(st[m][stage_off<N, SW>(s, k)]) << 1) : 0u;
-    int pos[IM], step[IM];
-    unsigned tie[IM], top[IM];
+        for (int k = 0; k < N; k++) ek[m][k] = (s < N) ? (fast_key(st[m][stage_off<N, SW>(s, k)]) << 1) : 0u;
+    int pos[IM];
+    unsigned top[IM];
 #pragma unroll
     for (int m = 0; m < IM; m++) {
         pos[m] = (s < N) ? s : 31;     // padding lanes: key 0, never on the diagonal
-        step[m] = 0;
-        tie[m] = 0u;
         top[m] = 0u;
     }
 #pragma unroll
     for (int k = 0; k < N; ++k) {
         // positions whose tree slot (position - k - 1) survives at step k
-        constexpr unsigned kNone = 0u;
-        const unsigned surv = (k + 1 < 32) ? (unsigned)(((unsigned long long)kSurv << (k + 1)) & 0xffffffffull) : kNone;
+        const unsigned surv = (k + 1 < 32) ? (unsigned)(((unsigned long long)kSurv << (k + 1)) & 0xffffffffull) : 0u;
 #pragma unroll
         for (int m = 0; m < IM; m++) {
             const bool at = (pos[m] == k);
@@ -455,24 +455,24 @@ __device__ __forceinline__ void replay_tracked_multi(const float* const (&st)[IM
             const unsigned mx = (P == 32) ? __reduce_max_sync(kFull, e) : group_max<P>(e);
             top[m] = max(top[m], mx);
             const bool hit = !at && (e == mx);
-            const unsigned tb = group_ballot<P>(hit, gbase);
-            tie[m] |= tb & (tb - 1u);
             int wpos;
-            if constexpr (P == 32) wpos = (int)__reduce_max_sync(kFull, hit ? (unsigned)pos[m] : 0u);
-            else wpos = __shfl_sync(kFull, pos[m], gbase + (tb ? __ffs(tb) - 1 : 0));
-            if (hit) {
-                pos[m] = k;
-                step[m] = k;
-            } else if (at) {
-                if (mx & 1u) step[m] = k;
-                else pos[m] = wpos;
+            if constexpr (P == 32) {
+                wpos = (int)__reduce_max_sync(kFull, hit ? (unsigned)pos[m] : 0u);
+            } else {
+                const unsigned tb = group_ballot<P>(hit, gbase);
+                wpos = __shfl_sync(kFull, pos[m], gbase + (tb ? __ffs(tb) - 1 : 0));
             }
+            if (hit) pos[m] = k;
+            else if (at && !(mx & 1u)) pos[m] = wpos;
         }
     }
 #pragma unroll
     for (int m = 0; m < IM; m++) {
-        const bool bad = (tie[m] != 0u) || (top[m] > kInfCode + 1u);
-        if (!bad && s < N) win[m][step[m]] = s;
+        // rows of one matrix (tagged by group) that ended on the same position
+        const unsigned same = __match_any_sync(kFull, pos[m] | (gbase << 8));
+        const bool dup = (s < N) && (__popc(same) > 1);
+        const bool bad = (group_ballot<P>(dup, gbase) != 0u) || (top[m] > kInfCode + 1u);
+        if (!bad && s < N) win[m][pos[m]] = s;
         if (__any_sync(kFull, bad)) replay_tracked<N, P, MODE, SW>(st[m], win[m], s, gbase);
     }
 }
