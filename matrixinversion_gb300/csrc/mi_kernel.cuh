@@ -101,13 +101,12 @@ struct Geom {
     // per-matrix scratch (floats)
     static constexpr int kCol = pad4(PR);
     static constexpr int kRow = pad4(PC);
-    static constexpr int kSwap = pad4(PC);
     static constexpr int oCol = 0;
     static constexpr int oRow = oCol + 2 * kCol;
-    static constexpr int oSwap = oRow + 2 * kRow;
-    static constexpr int oD = oSwap + 2 * kSwap;                        // pivot value of every step
+    static constexpr int oD = oRow + 2 * kRow;                          // pivot value of every step
     static constexpr int oWin = oD + 32;                                // input row placed at each step
-    static constexpr int kScratch = oWin + 32;
+    static constexpr int oMap = oWin + 32;                              // partial: output row of each slot
+    static constexpr int kScratch = oMap + 32;
 };
 
 // Stage layout of one matrix: row-major, with the TMA 128-byte swizzle
@@ -172,6 +171,17 @@ __device__ __forceinline__ unsigned group_max(unsigned x) {
     } else {
 #pragma unroll
         for (int o = P / 2; o > 0; o >>= 1) x = max(x, __shfl_xor_sync(kFull, x, o));
+        return x;
+    }
+}
+
+template <int P>
+__device__ __forceinline__ unsigned group_min(unsigned x) {
+    if constexpr (P == 32) {
+        return __reduce_min_sync(kFull, x);
+    } else {
+#pragma unroll
+        for (int o = P / 2; o > 0; o >>= 1) x = min(x, __shfl_xor_sync(kFull, x, o));
         return x;
     }
 }
@@ -550,19 +560,22 @@ __device__ __forceinline__ void set_row(float (&a)[G::R][G::C], int q, const flo
         }
 }
 
-// Partial pivoting (L = P: lane t of the group is logical row t): argmax of
-// the updated column over rows k.., first maximum; exchange rows k and r of
-// the register blocks through shared memory; then the same update.
-// ra: the input row held at logical row s.
+// Partial pivoting without row exchanges (L = P: lane t of the group keys
+// slot t, i.e. input row t).  Rows stay in their slots; each slot carries the
+// logical position lp it would have under getrf's physical exchanges, so the
+// argmax of the updated column k over the unplaced slots breaks ties toward
+// the lowest logical row exactly as LAPACK does.  The chosen slot's row is
+// the pivot row of the step (broadcast through shared memory); the slot that
+// holds logical row k takes over the winner's logical position.  The output
+// rows are permuted at the store (output row of a slot = the step that chose
+// it); the arithmetic of every row is that of the exchanging form.
 template <class G>
 __device__ __forceinline__ void gj_step_partial(float (&a)[G::R][G::C], float (&ps)[G::R], const int k, int rg, int cg,
-                                                int s, int gbase, float* scr, int& ra) {
+                                                int s, int gbase, float* scr, int& lp, bool& placed) {
     constexpr int R = G::R, C = G::C;
-    const int kr = k % G::RG, kri = k / G::RG;
     const int kc = k / C, kci = k % C;
     float* cb = scr + G::oCol + (k & 1) * G::kCol;
     float* rb = scr + G::oRow + (k & 1) * G::kRow;
-    float* sb = scr + G::oSwap + (k & 1) * G::kSwap;
     if (cg == kc) {
         float v[R];
 #pragma unroll
@@ -570,62 +583,45 @@ __device__ __forceinline__ void gj_step_partial(float (&a)[G::R][G::C], float (&
         sts_vec<R>(cb + rg * R, v);
     }
     __syncwarp();
-    // column entry of logical row t lives at cb[(t % RG) * R + t / RG]
+    // column entry of slot t lives at cb[(t % RG) * R + t / RG]
     unsigned key = 0u;
-    if (s >= k && s < G::kN) {
+    if (!placed && s < G::kN) {
         const unsigned b = __float_as_uint(cb[(s % G::RG) * R + s / G::RG]) & 0x7fffffffu;
         key = (b > 0x7f800000u) ? 1u : b + 2u;   // a NaN never beats a number
     }
     const unsigned mx = group_max<G::LL>(key);
-    const int r = __ffs(group_ballot<G::LL>(key != 0u && key == mx, gbase)) - 1;   // row k always competes
+    const bool top = (key != 0u) && (key == mx);
+    const unsigned lw = group_min<G::LL>(top ? (unsigned)lp : 0xffu);   // lowest logical row among the maxima
+    const int r = __ffs(group_ballot<G::LL>(top && (unsigned)lp == lw, gbase)) - 1;
+    if (s == r) {
+        lp = k;
+        placed = true;
+    } else if (lp == k) {
+        lp = (int)lw;
+    }
     const int rr = r % G::RG, rri = r / G::RG;
-    if (rg == rr) {           // row r becomes the pivot row
+    if (rg == rr) {           // slot r's row is the pivot row
         float w[C];
         get_row<G>(a, rri, w);
         sts_vec<C>(rb + cg * C, w);
     }
-    if (rg == kr) {           // row k moves to row r
-        float w[C];
-#pragma unroll
-        for (int ci = 0; ci < C; ci++) w[ci] = a[kri][ci];
-        sts_vec<C>(sb + cg * C, w);
-    }
     __syncwarp();
     float w[C];
     lds_vec<C>(rb + cg * C, w);
-    if (rg == kr) {
-#pragma unroll
-        for (int ci = 0; ci < C; ci++) a[kri][ci] = w[ci];
-    }
-    if (rg == rr && r != k) {
-        float t[C];
-        lds_vec<C>(sb + cg * C, t);
-        set_row<G>(a, rri, t);
-    }
     const float d = cb[rr * R + rri];
-    const float ck = cb[kr * R + kri];
     const float p = recip(d);
     if (s < G::kN) scr[G::oD + k] = d;    // every lane writes the same value
-    {
-        const int a_r = __shfl_sync(kFull, ra, gbase + r);
-        const int a_k = __shfl_sync(kFull, ra, gbase + k);
-        if (s == k) ra = a_r;
-        else if (s == r) ra = a_k;
-    }
+    if (s == 0) reinterpret_cast<int*>(scr + G::oWin)[k] = r;
     if (cg == kc) w[kci] = 1.0f;
     float c[R];
     lds_vec<R>(cb + rg * R, c);
 #pragma unroll
     for (int ri = 0; ri < R; ri++) {
-        const int row = rg + G::RG * ri;
-        c[ri] = (row == k) ? 0.0f : ((row == r) ? ck : c[ri]);
+        const bool piv = (rg + G::RG * ri == r);
+        c[ri] = piv ? 0.0f : c[ri];
+        ps[ri] = piv ? p : ps[ri];
+        if (cg == kc) a[ri][kci] = piv ? 1.0f : 0.0f;
     }
-    if (cg == kc) {
-#pragma unroll
-        for (int ri = 0; ri < R; ri++) a[ri][kci] = 0.0f;
-        if (rg == kr) a[kri][kci] = 1.0f;
-    }
-    if (rg == kr) ps[kri] = p;
 #pragma unroll
     for (int ri = 0; ri < R; ri++) row_update<C>(a[ri], c[ri] * p, w);
 }
@@ -642,7 +638,9 @@ __device__ __forceinline__ void gj_step_partial(float (&a)[G::R][G::C], float (&
 template <int N, int L, int MODE>
 struct KGeom {
     using G = Geom<N, L>;
-    static constexpr int H = (G::RG >= 8) ? 1 : 8 / G::RG;      // register rows per output round
+    // register rows per output round; partial pivoting permutes its output
+    // rows, so all of them leave in one round
+    static constexpr int H = (MODE == kModePartial) ? G::R : ((G::RG >= 8) ? 1 : 8 / G::RG);
     static constexpr int ORows = G::RG * H;                      // matrix rows per output round
     static constexpr int Rounds = (G::R + H - 1) / H;
     // Output rows leave in rounds of ORows rows per matrix, either as tensor
@@ -652,7 +650,9 @@ struct KGeom {
     static constexpr int OBR = ORows < N ? ORows : N;
     static constexpr int SB = (N % 4 == 0) ? (N <= 8 ? 8 : 40) : (N | 1);
     static constexpr int kSlot = G::M * G::kMat;
-    static constexpr int kOutT = G::M * OBR * N;                  // one tensor-store buffer
+    // one tensor-store buffer, a multiple of 128 bytes so that the second of
+    // the two alternating buffers starts on the alignment TMA tensor copies need
+    static constexpr int kOutT = (G::M * OBR * N + 31) & ~31;
     static constexpr int kOutS = G::M * ORows * SB;
     // Window copies (n not a multiple of 4): the group arrives as one 1-D bulk
     // copy of the 16-byte-aligned window around it (up to 3 floats of shift
@@ -666,7 +666,7 @@ struct KGeom {
     static constexpr int kOutW = G::M * kOWm;
     static constexpr int kOut0 = (2 * kOutT > kOutS) ? 2 * kOutT : kOutS;
     static constexpr int kOut = (WinStore && 2 * kOutW > kOut0) ? 2 * kOutW : kOut0;
-    static constexpr int kScr = (MODE == kModePartial) ? G::kScratch : 64;   // partial needs the exchange buffers
+    static constexpr int kScr = (MODE == kModePartial) ? G::kScratch : 64;   // partial: column/row buffers, row map
     static constexpr int kScrTotal = G::M * kScr;
     static constexpr int r4(int x) { return (x + 3) & ~3; }
     // per-warp region (floats): slot | output rows | scratch | mbarrier; the
@@ -676,6 +676,8 @@ struct KGeom {
     static constexpr int oScr = oOut + r4(kOut);
     static constexpr int oBar = oScr + r4(kScrTotal);
     static constexpr int kWarp = (oBar + 4 + 255) / 256 * 256;   // 1 KB multiple
+    static_assert(kOutT % 32 == 0 && oOut % 32 == 0, "TMA tensor-store buffers must start on 128-byte boundaries");
+    static_assert(N != 32 || (kOutT % 256 == 0 && oOut % 256 == 0), "128-byte-swizzled buffers need 1 KB alignment");
 };
 
 // Offsets of the small per-matrix scratch: pivot values, then pivot rows.
@@ -784,10 +786,13 @@ __device__ __forceinline__ void phase_eliminate(float (&a)[GeomN<N, L, MODE>::R]
 #pragma unroll
     for (int ri = 0; ri < R; ri++) ps[ri] = 1.0f;
     if constexpr (MODE == kModePartial) {
-        int ra = s;
+        int lp = s;
+        bool placed = (s >= N);
 #pragma unroll
-        for (int k = 0; k < N; ++k) gj_step_partial<G>(a, ps, k, rg, cg, s, mslot * L, scr, ra);
-        if (s < N) reinterpret_cast<int*>(scr + G::oWin)[s] = ra;
+        for (int k = 0; k < N; ++k) gj_step_partial<G>(a, ps, k, rg, cg, s, mslot * L, scr, lp, placed);
+        __syncwarp();
+        // output row of each slot = the step that chose it
+        if (s < N) reinterpret_cast<int*>(scr + G::oMap)[reinterpret_cast<const int*>(scr + G::oWin)[s]] = s;
     } else {
 #pragma unroll
         for (int k = 0; k < N; ++k) gj_step<G>(a, ps, k, rg, cg, mslot * L, scr);
@@ -842,12 +847,13 @@ __device__ __forceinline__ void phase_store_tensor(const float (&a)[GeomN<N, L, 
         float* ob = obuf + mslot * K::OBR * N;
         if (lane == 0) bulk_wait_read_one();   // this buffer's store from two rounds ago has read it
         __syncwarp();
+        const int* omap = reinterpret_cast<const int*>(scr0 + mslot * K::kScr + G::oMap);
 #pragma unroll
         for (int h = 0; h < K::H; h++) {
             const int ri = q * K::H + h;
-            const int lr = rg + G::RG * h;
+            const int i = rg + G::RG * ri;
+            const int lr = (MODE == kModePartial) ? ((ri < R && i < N) ? omap[i] : K::OBR) : rg + G::RG * h;
             if (ri < R && lr < K::OBR) {
-                const int i = rg + G::RG * ri;
                 if (i < N) {
                     float* orow = ob + lr * N;
                     const int x = (N == 32) ? ((lr & 7) << 2) : 0;
@@ -960,7 +966,10 @@ __device__ __forceinline__ void phase_store_rows(const float (&a)[GeomN<N, L, MO
             if (ri < R) {
                 const int i = rg + G::RG * ri;
                 if (i < N) {
-                    float* orow = ob + (rg + G::RG * h) * K::SB;
+                    const int lr = (MODE == kModePartial)
+                                       ? reinterpret_cast<const int*>(scr0 + mslot * K::kScr + G::oMap)[i]
+                                       : rg + G::RG * h;
+                    float* orow = ob + lr * K::SB;
 #pragma unroll
                     for (int ci = 0; ci < C; ci++)
                         if (cg * C + ci < N) orow[dst[ci]] = a[ri][ci];

@@ -102,7 +102,7 @@ def test_subnormals_compare_as_zero(mi_gpu, oracle, n):
     assert np.array_equal(p, oracle.pivots(A, "reference"))
 
 
-@pytest.mark.parametrize("n", [2, 5, 9, 16, 24, 32])
+@pytest.mark.parametrize("n", [2, 5, 9, 12, 16, 20, 24, 28, 32])
 def test_partial_pivoting(mi_gpu, oracle, n):
     A = oracle.uniform(300 + n, 2000, n)
     X, perm, info = gpu_inverse(mi_gpu, A, "partial")
