@@ -881,7 +881,7 @@ __device__ __forceinline__ void phase_store_tensor(const float (&a)[GeomN<N, L, 
 template <int N, int L, int MODE>
 __device__ __forceinline__ void phase_store_window(const float (&a)[GeomN<N, L, MODE>::R][GeomN<N, L, MODE>::C],
                                                    float* outb, const float* scr0, int lane, float* A,
-                                                   long long first, long long batch, unsigned& round) {
+                                                   const long long (&gbase)[GeomN<N, L, MODE>::M], unsigned& round) {
     using G = GeomN<N, L, MODE>;
     using K = KGeom<N, L, MODE>;
     constexpr int R = G::R, C = G::C, M = G::M;
@@ -898,7 +898,7 @@ __device__ __forceinline__ void phase_store_window(const float (&a)[GeomN<N, L, 
         float* obuf = outb + par * K::kOutW;
         if (lane == 0) bulk_wait_read_one();
         __syncwarp();
-        const int e = (int)(((first + mslot) * NN + (long long)row0 * N) & 3);
+        const int e = (int)((gbase[mslot] + (long long)row0 * N) & 3);   // (gbase < 0: no matrix, value unused)
         float* ob = obuf + mslot * K::kOWm + e;
 #pragma unroll
         for (int h = 0; h < K::H; h++) {
@@ -918,8 +918,8 @@ __device__ __forceinline__ void phase_store_window(const float (&a)[GeomN<N, L, 
         if (lane == 0) {
 #pragma unroll
             for (int m = 0; m < M; m++) {
-                if (first + m < batch) {
-                    const long long g0 = (first + m) * NN + (long long)row0 * N, g1 = g0 + (long long)rows * N;
+                if (gbase[m] >= 0) {
+                    const long long g0 = gbase[m] + (long long)row0 * N, g1 = g0 + (long long)rows * N;
                     const long long a0 = (g0 + 3) & ~3LL, a1 = g1 & ~3LL;
                     if (a1 > a0)
                         bulk_store(A + a0, obuf + m * K::kOWm + (int)(g0 & 3) + (int)(a0 - g0),
@@ -930,8 +930,12 @@ __device__ __forceinline__ void phase_store_window(const float (&a)[GeomN<N, L, 
         }
         for (int t = lane; t < M * 6; t += 32) {
             const int m = t / 6, u = t - m * 6;
-            if (first + m < batch) {
-                const long long g0 = (first + m) * NN + (long long)row0 * N, g1 = g0 + (long long)rows * N;
+            long long gb = gbase[0];
+#pragma unroll
+            for (int q = 1; q < M; q++)
+                if (m == q) gb = gbase[q];
+            if (gb >= 0) {
+                const long long g0 = gb + (long long)row0 * N, g1 = g0 + (long long)rows * N;
                 const long long a0 = (g0 + 3) & ~3LL, a1 = g1 & ~3LL;
                 const long long head_end = a0 < g1 ? a0 : g1;
                 const long long x = (u < 3) ? g0 + u : ((a1 > a0 ? a1 : a0) + (u - 3));
@@ -1168,7 +1172,10 @@ __global__ void __launch_bounds__(256, 2) mi_inverse_kernel(float* __restrict__ 
         if (copy_mode == kCopyTensor) {
             phase_store_tensor<N, L, MODE>(a, sm.outb, sm.scr0, lane, &tmap_out, first, round);
         } else if (K::WinStore && copy_mode == kCopyWindow) {
-            phase_store_window<N, L, MODE>(a, sm.outb, sm.scr0, lane, A, first, batch, round);
+            long long gbase[M];
+#pragma unroll
+            for (int m = 0; m < M; m++) gbase[m] = (first + m < batch) ? (first + m) * NN : -1;
+            phase_store_window<N, L, MODE>(a, sm.outb, sm.scr0, lane, A, gbase, round);
         } else {
             float* gout[M];
 #pragma unroll
@@ -1253,6 +1260,7 @@ __global__ void __launch_bounds__(256, 2) mi_inverse_indexed_kernel(float* __res
 
     long long g = (long long)blockIdx.x * W + warp;
     uint32_t phase = 0;
+    unsigned round = 0;
     bool used_bar = false;
     if (g < groups) used_bar = issue(g);
     while (g < groups) {
@@ -1289,10 +1297,18 @@ __global__ void __launch_bounds__(256, 2) mi_inverse_indexed_kernel(float* __res
             used_bar = issue(gn);
         }
         phase_eliminate<N, L, MODE>(a, sm.scr0, lane);
-        phase_store_rows<N, L, MODE>(a, sm.outb, sm.scr0, lane, gout, vec);
+        if (K::WinStore && base16) {
+            long long gbase[M];
+#pragma unroll
+            for (int m = 0; m < M; m++) gbase[m] = idx[m] >= 0 ? offsets[idx[m]] : -1;
+            phase_store_window<N, L, MODE>(a, sm.outb, sm.scr0, lane, base, gbase, round);
+        } else {
+            phase_store_rows<N, L, MODE>(a, sm.outb, sm.scr0, lane, gout, vec);
+        }
         phase_perm_info<N, L, MODE>(sm.scr0, lane, idx[mslot], perm_out, 32, info_out);
         g = gn;
     }
+    if (lane == 0) bulk_wait_all();
 }
 
 // Dynamic shared memory for a block of `warps` warps (1 KB of slack for the
