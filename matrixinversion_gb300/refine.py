@@ -147,12 +147,44 @@ def study(per_bucket: int = 65536, kappas=KAPPAS, steps=(1, 2), seed: int = 0, t
     return out
 
 
+def bench_ns(count: int = 262144, steps: int = 1, iters: int = 5, seed: int = 0):
+    """Kernel time of `steps` Newton-Schulz steps on `count` matrices (no
+    library linear algebra involved: uniform inputs with +32 on the diagonal,
+    the starting inverse from the no-pivot kernel).  For profiling."""
+    import torch
+
+    import matrixinversion_gb300 as mi
+
+    g = torch.Generator(device="cuda").manual_seed(seed)
+    A = torch.rand(count, 32, 32, generator=g, device="cuda") * 2 - 1 + 32 * torch.eye(32, device="cuda")
+    X0, _, _ = mi.batched_inverse(A, "none")
+    bufs = [X0.clone() for _ in range(iters + 2)]
+    for b in bufs[:2]:
+        newton_schulz_(A, b, steps)
+    torch.cuda.synchronize()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    torch.cuda._sleep(200_000)
+    ev[0].record()
+    for b in bufs[2:]:
+        newton_schulz_(A, b, steps)
+    ev[1].record()
+    torch.cuda.synchronize()
+    ms = ev[0].elapsed_time(ev[1]) / iters
+    return {"count": count, "steps": steps, "ms": ms, "matrices_per_s": count / ms * 1e3,
+            "GBs": count * 12288 * steps / ms / 1e6}
+
+
 def main(argv=None):
     p = argparse.ArgumentParser()
     p.add_argument("--per-bucket", type=int, default=65536)
     p.add_argument("--seed", type=int, default=0)
     p.add_argument("--out", default=None)
+    p.add_argument("--ns-only", type=int, default=0, help="only time the Newton-Schulz kernel on this many matrices")
     a = p.parse_args(argv)
+    if a.ns_only:
+        for k in (1, 2):
+            print(json.dumps(bench_ns(a.ns_only, k, seed=a.seed)), flush=True)
+        return
     rows = study(a.per_bucket, seed=a.seed)
     for r in rows:
         print(json.dumps(r), flush=True)
