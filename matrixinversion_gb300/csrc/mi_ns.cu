@@ -102,16 +102,23 @@ __global__ void __launch_bounds__(128, 2) mi_ns_kernel(const float* __restrict__
         const bool valid = mat < batch;
         const float4* ga = reinterpret_cast<const float4*>(A + mat * 1024);
         const float4* gx = reinterpret_cast<const float4*>(X + mat * 1024);
-        // the previous tile's output stage (bh) has been read by its bulk store
+        // all of this tile's loads in flight at once, before waiting for the
+        // previous tile's output stage (bh) to be read by its bulk store
+        float4 ra[8], rx[8];
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+            const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+            ra[q] = valid ? ga[lane + 32 * q] : zero;
+            rx[q] = valid ? gx[lane + 32 * q] : zero;
+        }
         if (tid == 0) bulk_wait_read_all();
         __syncthreads();
-#pragma unroll 4
+#pragma unroll
         for (int q = 0; q < 8; q++) {
             const int f = lane + 32 * q;               // float4 index within the matrix
             const int r = f >> 3, c = (f & 7) * 4;
-            const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
-            const float4 a = valid ? ga[f] : zero;
-            const float4 x = valid ? gx[f] : zero;
+            const float4 a = ra[q];
+            const float4 x = rx[q];
             const int m = 32 * warp + r;
             put4(sm.ah, sm.al, off(m, c), a);
             put4(sm.xah, sm.xal, off(m, c), x);
