@@ -159,6 +159,16 @@ int mi_refine_fp64_f32(const float* d_a, float* d_x, const int32_t* d_list, int6
                        void* stream);
 
 /*
+ * As mi_refine_fp64_f32 with the residual R = I - A X in compensated
+ * float-float arithmetic on the FP32 pipes (exact products, TwoSum
+ * accumulation: about 44 significant bits) and X R in FP32 -- the same
+ * accuracy gain where kappa * u < 1, several times faster on GPUs whose FP64
+ * rate is low.
+ */
+int mi_refine_df_f32(const float* d_a, float* d_x, const int32_t* d_list, int64_t count, int64_t batch, int n,
+                     void* stream);
+
+/*
  * Threads per block used for size n and pivot mode whenever a call passes
  * threads_per_block = 0.  Ships with a table measured on GB300; set 0 to
  * restore that table's entry.

@@ -58,6 +58,23 @@ def refine_fp64_(A, X, index, stream=None):
     return X
 
 
+def refine_df_(A, X, index, stream=None):
+    """One refinement step with a float-float residual for the matrices
+    X[index] (in place): the accuracy of the FP64 step at FP32-pipe speed."""
+    import torch
+
+    if not (index.is_cuda and index.dtype == torch.int32 and index.is_contiguous()):
+        raise TypeError("index must be a contiguous CUDA int32 tensor")
+    n = A.shape[-1]
+    st = (stream or torch.cuda.current_stream(A.device)).cuda_stream
+    with torch.cuda.device(A.device):
+        status = _lib.load().mi_refine_df_f32(ctypes.c_void_p(A.data_ptr()), ctypes.c_void_p(X.data_ptr()),
+                                              ctypes.c_void_p(index.data_ptr()), index.numel(), A.shape[0], n,
+                                              ctypes.c_void_p(st))
+    _lib.check(status)
+    return X
+
+
 def flag_ill_conditioned(A, X, threshold: float = 1e4):
     """Indices (CUDA int32) of matrices whose estimate ||A||_inf ||X||_inf of
     the condition number is at least `threshold`: there an FP32 residual is
@@ -114,6 +131,35 @@ def study(per_bucket: int = 65536, kappas=KAPPAS, steps=(1, 2), seed: int = 0, t
         refine_fp64_(A, X, idx)
         e = rel_error(X, X64)
         row["ns1_fp64_flagged"] = {"median": float(e.median()), "max": float(e.max()), "flagged": int(idx.numel())}
+        # float-float residual steps on the flagged matrices, from the plain inverse
+        for nsteps in (1, 2):
+            X = X0.clone()
+            idx = flag_ill_conditioned(A, X)
+            for _ in range(nsteps):
+                refine_df_(A, X, idx)
+            e = rel_error(X, X64)
+            row[f"df{nsteps}_flagged"] = {"median": float(e.median()), "max": float(e.max()),
+                                          "flagged": int(idx.numel())}
+        # the refined form: partial-pivoting inverse, then two float-float
+        # steps for the matrices whose condition estimate is >= 100, timed end
+        # to end (flagging included) on a fresh copy
+        def refined(Ain):
+            Xr_, _, _ = mi.batched_inverse(Ain, "partial")
+            ix = flag_ill_conditioned(Ain, Xr_, threshold=100.0)
+            refine_df_(Ain, Xr_, ix)
+            refine_df_(Ain, Xr_, ix)
+            return Xr_, ix
+        refined(A)
+        torch.cuda.synchronize()
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        ev[0].record()
+        Xref, ix = refined(A)
+        ev[1].record()
+        torch.cuda.synchronize()
+        ms = ev[0].elapsed_time(ev[1])
+        e = rel_error(Xref, X64)
+        row["refined"] = {"median": float(e.median()), "max": float(e.max()), "flagged": int(ix.numel()),
+                          "ms": ms, "matrices_per_s": per_bucket / ms * 1e3}
         # the reference pivot rule's inverse, plain and after one NS step
         Xr, _, _ = mi.batched_inverse(A, "reference")
         e = rel_error(Xr, X64)
@@ -130,7 +176,8 @@ def study(per_bucket: int = 65536, kappas=KAPPAS, steps=(1, 2), seed: int = 0, t
     for label, fn in (("inverse_partial", lambda X: mi.batched_inverse_(X, "partial")),
                       ("inverse_reference", lambda X: mi.batched_inverse_(X, "reference")),
                       ("ns1", lambda X: newton_schulz_(A, X, 1)), ("ns2", lambda X: newton_schulz_(A, X, 2)),
-                      ("fp64_all", lambda X: refine_fp64_(A, X, all_idx))):
+                      ("fp64_all", lambda X: refine_fp64_(A, X, all_idx)),
+                      ("df_all", lambda X: refine_df_(A, X, all_idx))):
         bufs = [(A if label.startswith("inverse") else X0).clone() for _ in range(timing_iters + 2)]
         for b in bufs[:2]:
             fn(b)

@@ -145,3 +145,33 @@ def test_fp64_step_on_flagged(mi_gpu, oracle):
     e0 = np.abs(x0 - X64).max((1, 2)) / np.abs(X64).max((1, 2))
     assert e[64:].max() <= 1e-5 and e0[64:].max() > 1e-4, (e[64:].max(), e0[64:].max())
     assert np.array_equal(x[:64], x0[:64])
+
+
+def test_float_float_step_matches_fp64_step(mi_gpu, oracle):
+    """The float-float residual step reaches the FP64 step's accuracy: at
+    kappa = 1e5, max |X - X64| <= 2e-6 * max |X64| after one step from the plain
+    inverse (FP64 step: same bound), <= 1e-6 after two."""
+    import torch
+
+    from matrixinversion_gb300 import refine
+
+    A = _inputs(1e5, 256, 31)
+    X0, _, _ = mi_gpu.batched_inverse(A, "partial")
+    idx = torch.arange(A.shape[0], dtype=torch.int32, device="cuda")
+    X64, _, _ = oracle.inverse_f64(A.cpu().numpy(), "partial")
+
+    def err(X):
+        x = X.cpu().numpy().astype(np.float64)
+        return np.abs(x - X64).max((1, 2)) / np.abs(X64).max((1, 2))
+
+    Xd = X0.clone()
+    refine.refine_df_(A, Xd, idx)
+    Xf = X0.clone()
+    refine.refine_fp64_(A, Xf, idx)
+    torch.cuda.synchronize()
+    ed, ef, e0 = err(Xd), err(Xf), err(X0)
+    assert e0.max() > 1e-4
+    assert ed.max() <= 2e-6 and ef.max() <= 2e-6, (ed.max(), ef.max())
+    refine.refine_df_(A, Xd, idx)
+    torch.cuda.synchronize()
+    assert err(Xd).max() <= 1e-6
