@@ -169,6 +169,15 @@ int mi_refine_df_f32(const float* d_a, float* d_x, const int32_t* d_list, int64_
                      void* stream);
 
 /*
+ * d_list[b] = b if ||A_b||_1 * ||X_b||_1 >= threshold (or is not finite),
+ * else -1, for b in [0, batch): a list the two refinement calls take as it is
+ * (count = batch; -1 entries are skipped), so flagging needs no host round
+ * trip.
+ */
+int mi_flag_condition_f32(const float* d_a, const float* d_x, int64_t batch, int n, float threshold,
+                          int32_t* d_list, void* stream);
+
+/*
  * Threads per block used for size n and pivot mode whenever a call passes
  * threads_per_block = 0.  Ships with a table measured on GB300; set 0 to
  * restore that table's entry.

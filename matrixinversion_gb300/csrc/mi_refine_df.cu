@@ -18,30 +18,43 @@ namespace mi {
 int set_cuda_error(cudaError_t e, const char* what);   // mi_api.cu
 int device_sm_count();
 
-constexpr int kDfWarps = 2;                             // 3 x 4.2 KB of staging per warp
-constexpr int kDfPitch = 33;                              // floats per staged row (bank spread)
+constexpr int kDfWarps = 2;                             // 4 staged 32 x 32 tiles per warp (about 17 KB)
+constexpr int kDfPitch = 33;                            // row-major tiles: column reads conflict-free
+constexpr int kDfPitchT = 34;                           // transposed tiles: 8-byte row-pair loads
 
-// (s, c) += a * x, exactly up to the final rounding of c.  Explicit
-// round-to-nearest intrinsics: none of these may be contracted into an FMA.
-__device__ __forceinline__ void df_madd(float& s, float& c, float a, float x) {
-    const float p = __fmul_rn(a, x);
-    const float e = fmaf(a, x, -p);                               // a * x = p + e exactly
-    const float t = __fadd_rn(s, p);                              // TwoSum(s, p) = t + r exactly
-    const float z = __fsub_rn(t, s);
-    const float r = __fadd_rn(__fsub_rn(s, __fsub_rn(t, z)), __fsub_rn(p, z));
+__device__ __forceinline__ float2 neg2(float2 v) { return make_float2(-v.x, -v.y); }
+
+// Two independent float-float accumulators (rows i and i + 1 of one column):
+// (s, c) += a * x with a = (a_i, a_i+1), x duplicated.  Packed FP32x2
+// arithmetic with explicit rounding (nothing contracted into an FMA).
+__device__ __forceinline__ void df_madd2(float2& s, float2& c, float2 a, float2 x) {
+    const float2 p = __fmul2_rn(a, x);
+    const float2 e = __ffma2_rn(a, x, neg2(p));                         // a * x = p + e exactly
+    const float2 t = __fadd2_rn(s, p);                                  // TwoSum(s, p) = t + r exactly
+    const float2 z = __fadd2_rn(t, neg2(s));
+    const float2 r = __fadd2_rn(__fadd2_rn(s, neg2(__fadd2_rn(t, neg2(z)))), __fadd2_rn(p, neg2(z)));
     s = t;
-    c = __fadd_rn(c, __fadd_rn(r, e));
+    c = __fadd2_rn(c, __fadd2_rn(r, e));
+}
+
+__device__ __forceinline__ float df_round(float s, float c, float d) {
+    const float t = __fadd_rn(s, d);
+    const float z = __fsub_rn(t, s);
+    const float r = __fadd_rn(__fsub_rn(s, __fsub_rn(t, z)), __fsub_rn(d, z));
+    return __fadd_rn(t, __fadd_rn(c, r));
 }
 
 __global__ void __launch_bounds__(64) mi_refine_df_kernel(const float* __restrict__ A, float* __restrict__ X,
-                                                           const int32_t* __restrict__ list, long long count,
-                                                           long long batch, int n) {
-    __shared__ float sa[kDfWarps][32 * kDfPitch];
-    __shared__ float sx[kDfWarps][32 * kDfPitch];
-    __shared__ float sr[kDfWarps][32 * kDfPitch];
+                                                          const int32_t* __restrict__ list, long long count,
+                                                          long long batch, int n) {
+    __shared__ float sat[kDfWarps][32 * kDfPitchT];    // A^T (row pair i, i+1 adjacent)
+    __shared__ float sxt[kDfWarps][32 * kDfPitchT];    // X^T
+    __shared__ float sx[kDfWarps][32 * kDfPitch];      // X
+    __shared__ float sr[kDfWarps][32 * kDfPitch];      // R
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const long long nn = (long long)n * n;
-    float* ma = sa[warp];
+    float* at = sat[warp];
+    float* xt = sxt[warp];
     float* mx = sx[warp];
     float* mr = sr[warp];
     for (long long t = (long long)blockIdx.x * kDfWarps + warp; t < count; t += (long long)gridDim.x * kDfWarps) {
@@ -52,37 +65,99 @@ __global__ void __launch_bounds__(64) mi_refine_df_kernel(const float* __restric
         for (int e = lane; e < 32 * 32; e += 32) {
             const int i = e >> 5, j = e & 31;
             const bool in = i < n && j < n;
-            ma[i * kDfPitch + j] = in ? a[i * n + j] : 0.0f;
-            mx[i * kDfPitch + j] = in ? x[i * n + j] : 0.0f;
+            const float av = in ? a[i * n + j] : 0.0f;
+            const float xv = in ? x[i * n + j] : 0.0f;
+            at[j * kDfPitchT + i] = av;
+            xt[j * kDfPitchT + i] = xv;
+            mx[i * kDfPitch + j] = xv;
         }
         __syncwarp();
         const int j = lane;
-        // column j of R = I - A X, accumulated as -(A X) + I in float-float
-        for (int i = 0; i < n; i++) {
-            float s = 0.0f, c = 0.0f;
-#pragma unroll 8
-            for (int k = 0; k < 32; k++) df_madd(s, c, -ma[i * kDfPitch + k], mx[k * kDfPitch + j]);
-            const float d = (i == j) ? 1.0f : 0.0f;
-            const float t2 = __fadd_rn(s, d);
-            const float z = __fsub_rn(t2, s);
-            const float r = __fadd_rn(__fsub_rn(s, __fsub_rn(t2, z)), __fsub_rn(d, z));
-            mr[i * kDfPitch + j] = __fadd_rn(t2, __fadd_rn(c, r));
+        // my column of X, each entry duplicated in a register pair
+        float2 xc[32];
+#pragma unroll
+        for (int k = 0; k < 32; k++) {
+            const float v = mx[k * kDfPitch + j];
+            xc[k] = make_float2(v, v);
+        }
+        // column j of R = I - A X, rows in pairs, accumulated as -(A X) + I in float-float
+        for (int i = 0; i < 32; i += 2) {
+            float2 s = make_float2(0.0f, 0.0f), c = make_float2(0.0f, 0.0f);
+#pragma unroll
+            for (int k = 0; k < 32; k++) {
+                const float2 ap = *reinterpret_cast<const float2*>(at + k * kDfPitchT + i);
+                df_madd2(s, c, neg2(ap), xc[k]);
+            }
+            mr[i * kDfPitch + j] = df_round(s.x, c.x, (i == j) ? 1.0f : 0.0f);
+            mr[(i + 1) * kDfPitch + j] = df_round(s.y, c.y, (i + 1 == j) ? 1.0f : 0.0f);
         }
         __syncwarp();
-        // column j of X + X R in FP32
-        if (j < n) {
-            for (int i = 0; i < n; i++) {
-                float s = 0.0f;
-#pragma unroll 8
-                for (int k = 0; k < 32; k++) s = fmaf(mx[i * kDfPitch + k], mr[k * kDfPitch + j], s);
-                x[i * n + j] = mx[i * kDfPitch + j] + s;
+        // column j of X + X R in FP32, rows in pairs
+        float2 rc[32];
+#pragma unroll
+        for (int k = 0; k < 32; k++) {
+            const float v = mr[k * kDfPitch + j];
+            rc[k] = make_float2(v, v);
+        }
+        for (int i = 0; i < 32; i += 2) {
+            float2 acc = make_float2(0.0f, 0.0f);
+#pragma unroll
+            for (int k = 0; k < 32; k++)
+                acc = __ffma2_rn(*reinterpret_cast<const float2*>(xt + k * kDfPitchT + i), rc[k], acc);
+            if (j < n) {
+                if (i < n) x[i * n + j] = mx[i * kDfPitch + j] + acc.x;
+                if (i + 1 < n) x[(i + 1) * n + j] = mx[(i + 1) * kDfPitch + j] + acc.y;
             }
         }
         __syncwarp();
     }
 }
 
+// list[b] = b if ||A_b||_1 * ||X_b||_1 >= threshold (a cheap estimate of the
+// condition number from the inverse itself), else -1.  One warp per matrix,
+// lane = column (coalesced rows), max of the column sums over the warp.
+__global__ void mi_flag_condition_kernel(const float* __restrict__ A, const float* __restrict__ X, long long batch,
+                                         int n, float threshold, int32_t* __restrict__ list) {
+    const int lane = threadIdx.x & 31;
+    const long long nn = (long long)n * n;
+    for (long long b = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; b < batch;
+         b += ((long long)gridDim.x * blockDim.x) >> 5) {
+        float ca = 0.0f, cx = 0.0f;
+        if (lane < n) {
+            const float* a = A + b * nn + lane;
+            const float* x = X + b * nn + lane;
+            for (int i = 0; i < n; i++) {
+                ca += fabsf(a[(long long)i * n]);
+                cx += fabsf(x[(long long)i * n]);
+            }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            ca = fmaxf(ca, __shfl_xor_sync(0xffffffffu, ca, o));
+            cx = fmaxf(cx, __shfl_xor_sync(0xffffffffu, cx, o));
+        }
+        const float est = ca * cx;
+        // a non-finite estimate (inf or NaN in the inverse) is flagged too
+        if (lane == 0) list[b] = (!(est < threshold)) ? (int32_t)b : -1;
+    }
+}
+
 }  // namespace mi
+
+extern "C" int mi_flag_condition_f32(const float* d_a, const float* d_x, int64_t batch, int n, float threshold,
+                                     int32_t* d_list, void* stream) {
+    if (n < 1 || n > 32 || batch < 0) return MI_ERR_INVALID_VALUE;
+    if (batch == 0) return MI_OK;
+    if (d_a == nullptr || d_x == nullptr || d_list == nullptr) return MI_ERR_NULL_POINTER;
+    long long blocks = (batch + 7) / 8;                   // 8 warps per block
+    const long long cap = 16LL * mi::device_sm_count();
+    if (blocks > cap) blocks = cap;
+    mi::mi_flag_condition_kernel<<<(unsigned)blocks, 256, 0, reinterpret_cast<cudaStream_t>(stream)>>>(
+        d_a, d_x, batch, n, threshold, d_list);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return mi::set_cuda_error(e, "condition flag launch");
+    return MI_OK;
+}
 
 extern "C" int mi_refine_df_f32(const float* d_a, float* d_x, const int32_t* d_list, int64_t count, int64_t batch,
                                 int n, void* stream) {

@@ -175,3 +175,18 @@ def test_float_float_step_matches_fp64_step(mi_gpu, oracle):
     refine.refine_df_(A, Xd, idx)
     torch.cuda.synchronize()
     assert err(Xd).max() <= 1e-6
+
+
+def test_device_flag_list_matches_host_flags(mi_gpu):
+    import torch
+
+    from matrixinversion_gb300 import refine
+
+    A = torch.cat([_inputs(1e1, 40, 41), _inputs(1e5, 40, 42)])
+    X, _, _ = mi_gpu.batched_inverse(A, "partial")
+    X[3] = float("nan")                                   # a non-finite inverse is flagged
+    lst = refine.flag_list(A, X, threshold=1e4).cpu().numpy()
+    want = set(refine.flag_ill_conditioned(A, X, threshold=1e4).cpu().numpy().tolist())
+    assert set(int(v) for v in lst if v >= 0) == want
+    assert all(v in (-1, b) for b, v in enumerate(lst))
+    assert 3 in want and set(range(40, 80)) <= want
