@@ -15,6 +15,11 @@ them first come, first served into a device pool with a fixed HBM budget:
   separate copy and compute streams so that consecutive batches overlap;
 * a request completes when the host sees its batch's last copy finish.
 
+With `resident=True` the requests' matrices already sit in HBM (produced by
+an upstream device stage): batches are inverted in place in the device ring,
+with no copies, and `offline()` gives the plain batched kernel's rate on the
+same matrices for comparison.
+
 The baseline ("per_request") runs the same loop with one request per batch
 and a plain contiguous launch per request.  Both paths run the same kernels
 on the same data, so results are equal bit for bit (tested).
@@ -116,7 +121,7 @@ class CudaServer:
     descriptor tables of the trace (built once on the device)."""
 
     def __init__(self, trace: Trace, hbm_budget_bytes: int = 16 << 30, device=None, pivot: int = PIVOT_PARTIAL,
-                 seed: int = 0):
+                 seed: int = 0, resident: bool = False):
         import torch
 
         from . import _lib
@@ -134,7 +139,10 @@ class CudaServer:
         if 8 * half > hbm_budget_bytes:
             raise ValueError("the largest request does not fit the HBM budget")
         self.half_floats = int(half)
-        self.arena = torch.empty(2 * self.half_floats, dtype=torch.float32, device=self.dev)
+        # resident: the requests' matrices already sit in HBM (an upstream
+        # device stage produced them) and are inverted in place, no copies
+        self.resident = resident
+        self.arena = None if resident else torch.empty(2 * self.half_floats, dtype=torch.float32, device=self.dev)
         # host rings (pinned): requests in arrival order, uniform [-1, 1)
         g = torch.Generator(device=self.dev).manual_seed(seed)
         src = torch.empty(total, dtype=torch.float32, device=self.dev)
@@ -144,8 +152,11 @@ class CudaServer:
             src[a:b] = torch.rand(b - a, generator=g, device=self.dev) * 2 - 1
         self.ring_in = torch.empty(total, dtype=torch.float32, pin_memory=True)
         self.ring_in.copy_(src)
-        del src
         self.ring_out = torch.empty(total, dtype=torch.float32, pin_memory=True)
+        if resident:
+            self.ring_dev = src                       # inverted in place, restored before each run
+            self.pristine = src.clone()
+        del src
         # descriptor tables of every matrix of the trace, in ring order, on the device
         k, n, off = trace.k, trace.n, trace.offset
         req_of = np.repeat(np.arange(len(k)), k)
@@ -173,12 +184,15 @@ class CudaServer:
         base = int(t.offset[i])
         end = int(t.offset[j - 1] + t.floats[j - 1])
         span = end - base
-        dst = self.arena[half * self.half_floats: half * self.half_floats + span]
-        ev_in = torch.cuda.Event()
-        with torch.cuda.stream(self.s_h2d):
-            dst.copy_(self.ring_in[base:end], non_blocking=True)
-            ev_in.record(self.s_h2d)
-        self.s_cmp.wait_event(ev_in)
+        if self.resident:
+            dst = self.ring_dev[base:end]
+        else:
+            dst = self.arena[half * self.half_floats: half * self.half_floats + span]
+            ev_in = torch.cuda.Event()
+            with torch.cuda.stream(self.s_h2d):
+                dst.copy_(self.ring_in[base:end], non_blocking=True)
+                ev_in.record(self.s_h2d)
+            self.s_cmp.wait_event(ev_in)
         st = ctypes.c_void_p(self.s_cmp.cuda_stream)
         m0 = int(self.mat_first[i])
         m1 = int(self.mat_first[j - 1] + t.k[j - 1])
@@ -210,6 +224,8 @@ class CudaServer:
                     self.check(status)
             ev_cmp = torch.cuda.Event()
             ev_cmp.record(self.s_cmp)
+        if self.resident:
+            return ev_cmp
         self.s_d2h.wait_event(ev_cmp)
         ev_out = torch.cuda.Event()
         with torch.cuda.stream(self.s_d2h):
@@ -229,6 +245,8 @@ class CudaServer:
         free = [0, 1]
         i = 0
         completed = 0
+        if self.resident:
+            self.ring_dev.copy_(self.pristine)
         self.torch.cuda.synchronize(self.dev)
         t0 = time.perf_counter()
         while completed < nreq:
@@ -251,7 +269,39 @@ class CudaServer:
         """Output matrices of request r (host copy of the output ring)."""
         t = self.trace
         o, kk, nn = int(t.offset[r]), int(t.k[r]), int(t.n[r])
+        if self.resident:
+            return self.ring_dev[o: o + kk * nn * nn].cpu().numpy().reshape(kk, nn, nn)
         return self.ring_out[o: o + kk * nn * nn].numpy().reshape(kk, nn, nn)
+
+    def offline(self, iters: int = 5) -> float:
+        """matrices/s of one descriptor call over the whole trace, resident in
+        HBM (the plain batched kernel on the same matrices, no serving)."""
+        torch = self.torch
+        t = self.trace
+        m = int(t.k.sum())
+        src = self.pristine if self.resident else None
+        if src is None:
+            src = torch.from_numpy(self.ring_in.numpy()).to(self.dev)
+        work = torch.empty_like(src)
+        st = ctypes.c_void_p(self.s_cmp.cuda_stream)
+        ts = []
+        for it in range(iters + 1):
+            work.copy_(src)
+            torch.cuda.synchronize(self.dev)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            with torch.cuda.stream(self.s_cmp):
+                torch.cuda._sleep(200_000)
+                e0.record()
+                self.check(self.L.mi_inverse_descr_f32(
+                    ctypes.c_void_p(work.data_ptr()), ctypes.c_void_p(self.d_off.data_ptr()),
+                    ctypes.c_void_p(self.d_n.data_ptr()), ctypes.c_void_p(self.d_flag.data_ptr()), None,
+                    ctypes.c_void_p(self.d_info.data_ptr()), m, self.n_mask, 1 << self.pivot,
+                    ctypes.c_void_p(self.ws.data_ptr()), self.ws.numel(), st))
+                e1.record()
+            torch.cuda.synchronize(self.dev)
+            if it > 0:
+                ts.append(e0.elapsed_time(e1))
+        return m / (float(np.median(ts)) / 1e3)
 
     def inputs(self, r: int):
         t = self.trace
@@ -266,16 +316,20 @@ def residual_max(A: np.ndarray, X: np.ndarray) -> float:
     return float(np.abs(R).sum(-1).max())
 
 
-def sweep(rates, num_requests: int, budget_gb: float = 16.0, seed: int = 0, modes=("coalesced", "per_request")):
+def sweep(rates, num_requests: int, budget_gb: float = 16.0, seed: int = 0, modes=("coalesced", "per_request"),
+          resident: bool = False):
     base = make_trace(num_requests, rates[0], seed=seed)
-    srv = CudaServer(base, hbm_budget_bytes=int(budget_gb * (1 << 30)), seed=seed)
+    srv = CudaServer(base, hbm_budget_bytes=int(budget_gb * (1 << 30)), seed=seed, resident=resident)
     out = []
     matrices = int(base.k.sum())
     srv.run(retime(base, rates[0], seed), coalesce=True)        # warm-up: module load, occupancy caches
+    plain = srv.offline()
+    print(json.dumps({"resident": resident, "offline_matrices_per_s": plain}), flush=True)
     sample = np.random.default_rng(seed).choice(num_requests, size=min(16, num_requests), replace=False)
     for rate in rates:
         tr = retime(base, rate, seed)
-        row = {"rate_rps": rate, "requests": num_requests, "matrices": matrices}
+        row = {"rate_rps": rate, "requests": num_requests, "matrices": matrices, "resident": resident,
+               "offline_matrices_per_s": plain}
         outs = {}
         for mode in modes:
             lat, wall = srv.run(tr, coalesce=(mode == "coalesced"))
@@ -298,8 +352,9 @@ def main(argv=None):
     p.add_argument("--budget-gb", type=float, default=16.0)
     p.add_argument("--seed", type=int, default=0)
     p.add_argument("--out", default=None)
+    p.add_argument("--resident", action="store_true", help="requests already in HBM: no host copies")
     a = p.parse_args(argv)
-    rows = sweep([float(x) for x in a.rates.split(",")], a.requests, a.budget_gb, a.seed)
+    rows = sweep([float(x) for x in a.rates.split(",")], a.requests, a.budget_gb, a.seed, resident=a.resident)
     if a.out:
         with open(a.out, "w") as f:
             json.dump(rows, f, indent=1)

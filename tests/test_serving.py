@@ -63,3 +63,18 @@ def test_coalesced_equals_alone(mi_gpu):
         X, _, _ = mi_gpu.batched_inverse(torch.from_numpy(A.copy()).cuda(), "partial")
         assert np.array_equal(X.cpu().numpy(), mixed[r]), r
     assert serving.residual_max(srv.inputs(0), mixed[0]) < 1e-2
+
+
+@pytest.mark.gpu
+def test_resident_mode_equals_host_mode(mi_gpu):
+    """Requests already in HBM, inverted in place: same bits as the host-ring path."""
+    t = serving.make_trace(40, 20000.0, seed=13, kmax=64)
+    host = serving.CudaServer(t, hbm_budget_bytes=1 << 28, seed=13)
+    res = serving.CudaServer(t, hbm_budget_bytes=1 << 28, seed=13, resident=True)
+    host.run(coalesce=True)
+    for _ in range(2):                         # the ring is restored before every run
+        lat, wall = res.run(coalesce=True)
+        assert np.all(np.isfinite(lat)) and wall > 0
+        for r in range(40):
+            assert np.array_equal(res.results(r), host.results(r)), r
+    assert res.offline(iters=2) > 0
