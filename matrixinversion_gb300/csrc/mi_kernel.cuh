@@ -336,19 +336,17 @@ __device__ __forceinline__ unsigned group_max_redux(unsigned x, int gbase) {
 // the reduction latencies of the chains overlap; keys are read from the
 // stage four columns at a time (a compact, rolled loop).  A step costs one
 // group maximum: the lane holding it takes the step, with no per-step vote or
-// branch.  A matrix whose maximum ever tied (two rows placed in one step,
-// so a later step finds only placed rows, key 0, and they take it again) or
-// where a NaN competed is replayed afterwards with the exact rule.
+// branch.  A matrix whose maximum ever tied (found at the end: two rows on one
+// step) or where a NaN competed is replayed afterwards with the exact rule.
 template <int N, int P, int IM, int MODE, bool SW = (N == 32)>
 __device__ __forceinline__ void replay_fast_multi(const float* const (&st)[IM], int* const (&win)[IM], int s,
                                                   int gbase) {
-    bool placed[IM], dup[IM];
+    bool placed[IM];
     int step[IM];
     unsigned top[IM];
 #pragma unroll
     for (int m = 0; m < IM; m++) {
         placed[m] = (s >= N);
-        dup[m] = false;
         step[m] = 0;
         top[m] = 0u;
     }
@@ -366,7 +364,6 @@ __device__ __forceinline__ void replay_fast_multi(const float* const (&st)[IM], 
                     const unsigned cand = placed[m] ? 0u : kv[m][t];
                     const unsigned mx = group_max_redux<P>(cand, gbase);
                     const bool hit = (cand == mx);
-                    dup[m] = dup[m] || (hit && placed[m]);
                     top[m] = max(top[m], mx);
                     if (hit) {
                         placed[m] = true;
@@ -378,7 +375,13 @@ __device__ __forceinline__ void replay_fast_multi(const float* const (&st)[IM], 
     }
 #pragma unroll
     for (int m = 0; m < IM; m++) {
-        const bool bad = (group_ballot<P>(dup[m], gbase) != 0u) || (top[m] > 0x7f800000u);
+        // every row takes exactly one step unless a maximum tied (two rows in
+        // one step, or placed rows taking a later step where only keys 0
+        // remain): rows that ended on one step are found by one match
+        const int tag = ((s < N) ? step[m] : 64 + s) | (gbase << 8);
+        const unsigned same = __match_any_sync(kFull, tag);   // every lane takes part
+        const bool dup = (s < N) && (__popc(same) > 1);
+        const bool bad = (group_ballot<P>(dup, gbase) != 0u) || (top[m] > 0x7f800000u);
         if (!bad && s < N) win[m][step[m]] = s;
         if (__any_sync(kFull, bad)) {
 #pragma unroll 1
@@ -837,6 +840,16 @@ __device__ __forceinline__ void phase_store_tensor(const float (&a)[GeomN<N, L, 
     const int rg = s % G::RG, cg = s / G::RG;
     int dst[C];
     dest_columns<N, L, MODE>(dst, scr0, lane);
+    // n = 32 (128-byte swizzle): with 4 row groups the swizzle of output row
+    // rg + 4h takes two values, one per parity of h -- two column tables
+    constexpr bool kTwoTables = (N == 32) && (G::RG == 4) && (MODE != kModePartial);
+    int dsx[kTwoTables ? 2 : 1][C];
+    if constexpr (kTwoTables) {
+#pragma unroll
+        for (int par = 0; par < 2; par++)
+#pragma unroll
+            for (int ci = 0; ci < C; ci++) dsx[par][ci] = dst[ci] ^ (((rg + 4 * par) & 7) << 2);
+    }
 #pragma unroll
     for (int q = 0; q < K::Rounds; q++) {
         // buffers alternate over the warp's whole sequence of rounds, so the
@@ -856,10 +869,15 @@ __device__ __forceinline__ void phase_store_tensor(const float (&a)[GeomN<N, L, 
             if (ri < R && lr < K::OBR) {
                 if (i < N) {
                     float* orow = ob + lr * N;
-                    const int x = (N == 32) ? ((lr & 7) << 2) : 0;
+                    if constexpr (kTwoTables) {
 #pragma unroll
-                    for (int ci = 0; ci < C; ci++)
-                        if (cg * C + ci < N) orow[dst[ci] ^ x] = a[ri][ci];
+                        for (int ci = 0; ci < C; ci++) orow[dsx[h & 1][ci]] = a[ri][ci];
+                    } else {
+                        const int x = (N == 32) ? ((lr & 7) << 2) : 0;
+#pragma unroll
+                        for (int ci = 0; ci < C; ci++)
+                            if (cg * C + ci < N) orow[dst[ci] ^ x] = a[ri][ci];
+                    }
                 }
             }
         }
