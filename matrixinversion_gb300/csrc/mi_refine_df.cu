@@ -80,16 +80,22 @@ __global__ void __launch_bounds__(64) mi_refine_df_kernel(const float* __restric
             const float v = mx[k * kDfPitch + j];
             xc[k] = make_float2(v, v);
         }
-        // column j of R = I - A X, rows in pairs, accumulated as -(A X) + I in float-float
-        for (int i = 0; i < 32; i += 2) {
-            float2 s = make_float2(0.0f, 0.0f), c = make_float2(0.0f, 0.0f);
+        // column j of R = I - A X, rows in pairs, accumulated as -(A X) + I in
+        // float-float; two row pairs at a time, so two TwoSum chains overlap
+        for (int i = 0; i < 32; i += 4) {
+            float2 s0 = make_float2(0.0f, 0.0f), c0 = make_float2(0.0f, 0.0f);
+            float2 s1 = make_float2(0.0f, 0.0f), c1 = make_float2(0.0f, 0.0f);
 #pragma unroll
             for (int k = 0; k < 32; k++) {
-                const float2 ap = *reinterpret_cast<const float2*>(at + k * kDfPitchT + i);
-                df_madd2(s, c, neg2(ap), xc[k]);
+                const float2 a0 = *reinterpret_cast<const float2*>(at + k * kDfPitchT + i);
+                const float2 a1 = *reinterpret_cast<const float2*>(at + k * kDfPitchT + i + 2);
+                df_madd2(s0, c0, neg2(a0), xc[k]);
+                df_madd2(s1, c1, neg2(a1), xc[k]);
             }
-            mr[i * kDfPitch + j] = df_round(s.x, c.x, (i == j) ? 1.0f : 0.0f);
-            mr[(i + 1) * kDfPitch + j] = df_round(s.y, c.y, (i + 1 == j) ? 1.0f : 0.0f);
+            mr[i * kDfPitch + j] = df_round(s0.x, c0.x, (i == j) ? 1.0f : 0.0f);
+            mr[(i + 1) * kDfPitch + j] = df_round(s0.y, c0.y, (i + 1 == j) ? 1.0f : 0.0f);
+            mr[(i + 2) * kDfPitch + j] = df_round(s1.x, c1.x, (i + 2 == j) ? 1.0f : 0.0f);
+            mr[(i + 3) * kDfPitch + j] = df_round(s1.y, c1.y, (i + 3 == j) ? 1.0f : 0.0f);
         }
         __syncwarp();
         // column j of X + X R in FP32, rows in pairs
