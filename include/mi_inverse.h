@@ -169,6 +169,18 @@ int mi_refine_df_f32(const float* d_a, float* d_x, const int32_t* d_list, int64_
                      void* stream);
 
 /*
+ * As mi_refine_df_f32, and also writes d_next[t] = d_list[t] where the
+ * error left after this step, estimated as max|X R^2| / max|X| (X and R
+ * before the step: X (I + R) - A^-1 = -A^-1 R^2 to first order), exceeds tol
+ * or is not finite, else -1 (also -1 for skipped entries).  d_next has count
+ * entries and may be d_list itself; it is the list for a second step, so that
+ * step runs only where the first does not suffice.  No counterpart in the
+ * reference.
+ */
+int mi_refine_df_next_f32(const float* d_a, float* d_x, const int32_t* d_list, int64_t count, int64_t batch, int n,
+                          float tol, int32_t* d_next, void* stream);
+
+/*
  * d_list[b] = b if ||A_b||_1 * ||X_b||_1 >= threshold (or is not finite),
  * else -1, for b in [0, batch): a list the two refinement calls take as it is
  * (count = batch; -1 entries are skipped), so flagging needs no host round

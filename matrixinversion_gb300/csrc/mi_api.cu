@@ -83,6 +83,22 @@ int device_sm_count() {
     return sms;
 }
 
+// Grid of a grid-stride kernel: as many blocks as are resident at once on the
+// current device (at most `want`), so that no partial second wave runs after
+// the first.  cache: one entry per device, 0 = not queried yet.
+long long resident_grid(const void* kernel, int threads, long long want, int* cache) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) dev = -1;
+    int per_sm = (dev >= 0 && dev < 64) ? cache[dev] : 0;
+    if (per_sm <= 0) {
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, 0) != cudaSuccess || per_sm < 1)
+            per_sm = 1;
+        if (dev >= 0 && dev < 64) cache[dev] = per_sm;
+    }
+    const long long cap = (long long)per_sm * device_sm_count();
+    return want < cap ? want : cap;
+}
+
 PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
     static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
     static std::once_flag once;

@@ -14,6 +14,7 @@ namespace mi {
 
 int set_cuda_error(cudaError_t e, const char* what);   // mi_api.cu
 int device_sm_count();
+long long resident_grid(const void* kernel, int threads, long long want, int* cache);
 
 constexpr int kR64Warps = 2;                          // 2 x 16.9 KB of FP64 staging per block
 constexpr int kR64Pitch = 33;                           // doubles per staged row (bank spread)
@@ -73,9 +74,9 @@ extern "C" int mi_refine_fp64_f32(const float* d_a, float* d_x, const int32_t* d
     if (n < 1 || n > 32 || count < 0 || batch < 0) return MI_ERR_INVALID_VALUE;
     if (count == 0) return MI_OK;
     if (d_a == nullptr || d_x == nullptr || d_list == nullptr) return MI_ERR_NULL_POINTER;
-    long long blocks = (count + mi::kR64Warps - 1) / mi::kR64Warps;
-    const long long cap = 8LL * mi::device_sm_count();
-    if (blocks > cap) blocks = cap;
+    static int per_sm[64] = {0};
+    const long long blocks = mi::resident_grid(reinterpret_cast<const void*>(mi::mi_refine64_kernel),
+                                               32 * mi::kR64Warps, (count + mi::kR64Warps - 1) / mi::kR64Warps, per_sm);
     mi::mi_refine64_kernel<<<(unsigned)blocks, 32 * mi::kR64Warps, 0, reinterpret_cast<cudaStream_t>(stream)>>>(
         d_a, d_x, d_list, count, batch, n);
     cudaError_t e = cudaGetLastError();

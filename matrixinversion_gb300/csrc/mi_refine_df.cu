@@ -17,8 +17,9 @@ namespace mi {
 
 int set_cuda_error(cudaError_t e, const char* what);   // mi_api.cu
 int device_sm_count();
+long long resident_grid(const void* kernel, int threads, long long want, int* cache);
 
-constexpr int kDfWarps = 2;                             // 4 staged 32 x 32 tiles per warp (about 17 KB)
+constexpr int kDfWarps = 2;                             // 3 staged 32 x 32 tiles per warp (about 13 KB)
 constexpr int kDfPitch = 33;                            // row-major tiles: column reads conflict-free
 constexpr int kDfPitchT = 34;                           // transposed tiles: 8-byte row-pair loads
 
@@ -45,40 +46,43 @@ __device__ __forceinline__ float df_round(float s, float c, float d) {
 }
 
 __global__ void __launch_bounds__(64) mi_refine_df_kernel(const float* __restrict__ A, float* __restrict__ X,
-                                                          const int32_t* __restrict__ list, long long count,
-                                                          long long batch, int n) {
-    __shared__ float sat[kDfWarps][32 * kDfPitchT];    // A^T (row pair i, i+1 adjacent)
+                                                          const int32_t* list, long long count, long long batch,
+                                                          int n, float tol, int32_t* next) {
+    __shared__ float sat[kDfWarps][32 * kDfPitchT];    // A^T (row pair i, i+1 adjacent), then the correction D^T
     __shared__ float sxt[kDfWarps][32 * kDfPitchT];    // X^T
-    __shared__ float sx[kDfWarps][32 * kDfPitch];      // X
     __shared__ float sr[kDfWarps][32 * kDfPitch];      // R
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const long long nn = (long long)n * n;
     float* at = sat[warp];
     float* xt = sxt[warp];
-    float* mx = sx[warp];
     float* mr = sr[warp];
     for (long long t = (long long)blockIdx.x * kDfWarps + warp; t < count; t += (long long)gridDim.x * kDfWarps) {
-        const long long b = list[t];
-        if (b < 0 || b >= batch) continue;                // out-of-range entries are skipped
+        // lane 0 alone reads list[t] and writes next[t], in that order, so the
+        // two may be one array
+        const long long b = __shfl_sync(0xffffffffu, lane == 0 ? (long long)list[t] : 0LL, 0);
+        if (b < 0 || b >= batch) {                        // out-of-range entries are skipped
+            if (next != nullptr && lane == 0) next[t] = -1;
+            continue;
+        }
         const float* a = A + b * nn;
         float* x = X + b * nn;
         for (int e = lane; e < 32 * 32; e += 32) {
             const int i = e >> 5, j = e & 31;
             const bool in = i < n && j < n;
-            const float av = in ? a[i * n + j] : 0.0f;
-            const float xv = in ? x[i * n + j] : 0.0f;
-            at[j * kDfPitchT + i] = av;
-            xt[j * kDfPitchT + i] = xv;
-            mx[i * kDfPitch + j] = xv;
+            at[j * kDfPitchT + i] = in ? a[i * n + j] : 0.0f;
+            xt[j * kDfPitchT + i] = in ? x[i * n + j] : 0.0f;
         }
         __syncwarp();
         const int j = lane;
         // my column of X, each entry duplicated in a register pair
         float2 xc[32];
+        float xmax = 0.0f;
 #pragma unroll
-        for (int k = 0; k < 32; k++) {
-            const float v = mx[k * kDfPitch + j];
-            xc[k] = make_float2(v, v);
+        for (int k = 0; k < 32; k += 2) {
+            const float2 v = *reinterpret_cast<const float2*>(xt + j * kDfPitchT + k);
+            xc[k] = make_float2(v.x, v.x);
+            xc[k + 1] = make_float2(v.y, v.y);
+            xmax = fmaxf(xmax, fmaxf(fabsf(v.x), fabsf(v.y)));
         }
         // column j of R = I - A X, rows in pairs, accumulated as -(A X) + I in
         // float-float; two row pairs at a time, so two TwoSum chains overlap
@@ -97,8 +101,9 @@ __global__ void __launch_bounds__(64) mi_refine_df_kernel(const float* __restric
             mr[(i + 2) * kDfPitch + j] = df_round(s1.x, c1.x, (i + 2 == j) ? 1.0f : 0.0f);
             mr[(i + 3) * kDfPitch + j] = df_round(s1.y, c1.y, (i + 3 == j) ? 1.0f : 0.0f);
         }
-        __syncwarp();
-        // column j of X + X R in FP32, rows in pairs
+        __syncwarp();                                      // R complete, A^T no longer read
+        // column j of X + X R in FP32, rows in pairs; the correction D = X R
+        // goes to the A^T tile (transposed) when the next-step estimate is wanted
         float2 rc[32];
 #pragma unroll
         for (int k = 0; k < 32; k++) {
@@ -110,10 +115,32 @@ __global__ void __launch_bounds__(64) mi_refine_df_kernel(const float* __restric
 #pragma unroll
             for (int k = 0; k < 32; k++)
                 acc = __ffma2_rn(*reinterpret_cast<const float2*>(xt + k * kDfPitchT + i), rc[k], acc);
+            const float2 xo = *reinterpret_cast<const float2*>(xt + j * kDfPitchT + i);   // X[i][j], X[i+1][j]
             if (j < n) {
-                if (i < n) x[i * n + j] = mx[i * kDfPitch + j] + acc.x;
-                if (i + 1 < n) x[(i + 1) * n + j] = mx[(i + 1) * kDfPitch + j] + acc.y;
+                if (i < n) x[i * n + j] = xo.x + acc.x;
+                if (i + 1 < n) x[(i + 1) * n + j] = xo.y + acc.y;
             }
+            if (next != nullptr) *reinterpret_cast<float2*>(at + j * kDfPitchT + i) = acc;
+        }
+        if (next != nullptr) {
+            __syncwarp();
+            // column j of D R = X R^2; the error left is about max|X R^2| / max|X|
+            float emax = 0.0f;
+            bool nan = false;
+            for (int i = 0; i < 32; i += 2) {
+                float2 acc = make_float2(0.0f, 0.0f);
+#pragma unroll
+                for (int k = 0; k < 32; k++)
+                    acc = __ffma2_rn(*reinterpret_cast<const float2*>(at + k * kDfPitchT + i), rc[k], acc);
+                nan = nan || isnan(acc.x) || isnan(acc.y);
+                emax = fmaxf(emax, fmaxf(fabsf(acc.x), fabsf(acc.y)));
+            }
+            float xm = xmax;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) xm = fmaxf(xm, __shfl_xor_sync(0xffffffffu, xm, o));
+            const bool bad = nan || !(emax <= tol * xm);   // inf fails the comparison too
+            const unsigned any = __ballot_sync(0xffffffffu, bad);
+            if (lane == 0) next[t] = any ? (int32_t)b : -1;
         }
         __syncwarp();
     }
@@ -165,17 +192,23 @@ extern "C" int mi_flag_condition_f32(const float* d_a, const float* d_x, int64_t
     return MI_OK;
 }
 
-extern "C" int mi_refine_df_f32(const float* d_a, float* d_x, const int32_t* d_list, int64_t count, int64_t batch,
-                                int n, void* stream) {
+extern "C" int mi_refine_df_next_f32(const float* d_a, float* d_x, const int32_t* d_list, int64_t count,
+                                     int64_t batch, int n, float tol, int32_t* d_next, void* stream) {
     if (n < 1 || n > 32 || count < 0 || batch < 0) return MI_ERR_INVALID_VALUE;
+    if (d_next != nullptr && !(tol >= 0.0f)) return MI_ERR_INVALID_VALUE;
     if (count == 0) return MI_OK;
     if (d_a == nullptr || d_x == nullptr || d_list == nullptr) return MI_ERR_NULL_POINTER;
-    long long blocks = (count + mi::kDfWarps - 1) / mi::kDfWarps;
-    const long long cap = 8LL * mi::device_sm_count();
-    if (blocks > cap) blocks = cap;
+    static int per_sm[64] = {0};
+    const long long blocks = mi::resident_grid(reinterpret_cast<const void*>(mi::mi_refine_df_kernel),
+                                               32 * mi::kDfWarps, (count + mi::kDfWarps - 1) / mi::kDfWarps, per_sm);
     mi::mi_refine_df_kernel<<<(unsigned)blocks, 32 * mi::kDfWarps, 0, reinterpret_cast<cudaStream_t>(stream)>>>(
-        d_a, d_x, d_list, count, batch, n);
+        d_a, d_x, d_list, count, batch, n, tol, d_next);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return mi::set_cuda_error(e, "float-float refinement launch");
     return MI_OK;
+}
+
+extern "C" int mi_refine_df_f32(const float* d_a, float* d_x, const int32_t* d_list, int64_t count, int64_t batch,
+                                int n, void* stream) {
+    return mi_refine_df_next_f32(d_a, d_x, d_list, count, batch, n, 0.0f, nullptr, stream);
 }

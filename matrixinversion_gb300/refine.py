@@ -21,6 +21,13 @@ import numpy as np
 from . import _lib
 
 KAPPAS = (1e1, 1e3, 1e5, 1e6)
+# The refined form's defaults.  An FP32 inverse of a 32 x 32 matrix can miss
+# 1e-6 relative error already at condition numbers of a few (max-norm error
+# about u * ||A||_1 ||X||_1), so every matrix whose estimate reaches 8 gets
+# one float-float step; a second step follows where the first leaves an
+# estimated error above 3e-7.
+REFINE_FLAG = 8.0
+REFINE_TOL = 3e-7
 
 
 def newton_schulz_(A, X, steps: int = 1, stream=None):
@@ -58,21 +65,40 @@ def refine_fp64_(A, X, index, stream=None):
     return X
 
 
-def refine_df_(A, X, index, stream=None):
+def refine_df_(A, X, index, stream=None, next_tol=None, next_out=None):
     """One refinement step with a float-float residual for the matrices
-    X[index] (in place): the accuracy of the FP64 step at FP32-pipe speed."""
+    X[index] (in place): the accuracy of the FP64 step at FP32-pipe speed.
+
+    With next_tol set, also returns the list for a second step: entry t is
+    index[t] where the error left after this step, estimated on the device as
+    max|X R^2| / max|X| (X, R = I - A X before the step), exceeds next_tol,
+    else -1.  next_out (CUDA int32, index.numel() entries) receives it and may
+    be `index` itself."""
     import torch
 
     if not (index.is_cuda and index.dtype == torch.int32 and index.is_contiguous()):
         raise TypeError("index must be a contiguous CUDA int32 tensor")
     n = A.shape[-1]
     st = (stream or torch.cuda.current_stream(A.device)).cuda_stream
+    lib = _lib.load()
     with torch.cuda.device(A.device):
-        status = _lib.load().mi_refine_df_f32(ctypes.c_void_p(A.data_ptr()), ctypes.c_void_p(X.data_ptr()),
-                                              ctypes.c_void_p(index.data_ptr()), index.numel(), A.shape[0], n,
-                                              ctypes.c_void_p(st))
+        if next_tol is None:
+            status = lib.mi_refine_df_f32(ctypes.c_void_p(A.data_ptr()), ctypes.c_void_p(X.data_ptr()),
+                                          ctypes.c_void_p(index.data_ptr()), index.numel(), A.shape[0], n,
+                                          ctypes.c_void_p(st))
+            _lib.check(status)
+            return X
+        if next_out is None:
+            next_out = torch.empty_like(index)
+        if not (next_out.is_cuda and next_out.dtype == torch.int32 and next_out.is_contiguous()
+                and next_out.numel() == index.numel()):
+            raise TypeError("next_out must be a contiguous CUDA int32 tensor shaped like index")
+        status = lib.mi_refine_df_next_f32(ctypes.c_void_p(A.data_ptr()), ctypes.c_void_p(X.data_ptr()),
+                                           ctypes.c_void_p(index.data_ptr()), index.numel(), A.shape[0], n,
+                                           float(next_tol), ctypes.c_void_p(next_out.data_ptr()),
+                                           ctypes.c_void_p(st))
     _lib.check(status)
-    return X
+    return next_out
 
 
 def flag_ill_conditioned(A, X, threshold: float = 1e4):
@@ -103,6 +129,23 @@ def flag_list(A, X, threshold: float = 1e4, out=None):
                                                    ctypes.c_void_p(st))
     _lib.check(status)
     return out
+
+
+def refined_inverse(A, flag_threshold: float = REFINE_FLAG, tol: float = REFINE_TOL, lists: bool = False):
+    """The refined form of batched_inverse(A, "partial"): the FP32
+    partial-pivoting inverse, one float-float-residual step for every matrix
+    whose condition estimate ||A||_1 ||X||_1 is at least flag_threshold, and a
+    second step only where the first leaves an estimated error above tol.
+    Flags and lists stay on the device (no host round trip).  Returns
+    (X, perm, info), plus the first and second step lists if `lists`."""
+    import matrixinversion_gb300 as mi
+
+    X, perm, info = mi.batched_inverse(A, "partial")
+    ix = flag_list(A, X, threshold=flag_threshold)
+    first = ix.clone() if lists else None
+    refine_df_(A, X, ix, next_tol=tol, next_out=ix)
+    refine_df_(A, X, ix)
+    return (X, perm, info, first, ix) if lists else (X, perm, info)
 
 
 def conditioned(batch: int, kappa: float, n: int = 32, seed: int = 0, device="cuda"):
@@ -159,26 +202,19 @@ def study(per_bucket: int = 65536, kappas=KAPPAS, steps=(1, 2), seed: int = 0, t
             e = rel_error(X, X64)
             row[f"df{nsteps}_flagged"] = {"median": float(e.median()), "max": float(e.max()),
                                           "flagged": int(idx.numel())}
-        # the refined form: partial-pivoting inverse, then two float-float
-        # steps for the matrices whose condition estimate is >= 100, timed end
-        # to end (flagging included) on a fresh copy
-        def refined(Ain):
-            Xr_, _, _ = mi.batched_inverse(Ain, "partial")
-            ix = flag_list(Ain, Xr_, threshold=100.0)
-            refine_df_(Ain, Xr_, ix)
-            refine_df_(Ain, Xr_, ix)
-            return Xr_, ix
-        refined(A)
+        # the refined form (refined_inverse), timed end to end on a fresh copy
+        _, _, _, first, second = refined_inverse(A, lists=True)
         torch.cuda.synchronize()
         ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
         ev[0].record()
-        Xref, ix = refined(A)
+        Xref, _, _ = refined_inverse(A)
         ev[1].record()
         torch.cuda.synchronize()
         ms = ev[0].elapsed_time(ev[1])
         e = rel_error(Xref, X64)
-        row["refined"] = {"median": float(e.median()), "max": float(e.max()), "flagged": int((ix >= 0).sum()),
-                          "ms": ms, "matrices_per_s": per_bucket / ms * 1e3}
+        row["refined"] = {"median": float(e.median()), "max": float(e.max()), "flagged": int((first >= 0).sum()),
+                          "second_step": int((second >= 0).sum()), "ms": ms,
+                          "matrices_per_s": per_bucket / ms * 1e3}
         # the reference pivot rule's inverse, plain and after one NS step
         Xr, _, _ = mi.batched_inverse(A, "reference")
         e = rel_error(Xr, X64)
@@ -196,7 +232,8 @@ def study(per_bucket: int = 65536, kappas=KAPPAS, steps=(1, 2), seed: int = 0, t
                       ("inverse_reference", lambda X: mi.batched_inverse_(X, "reference")),
                       ("ns1", lambda X: newton_schulz_(A, X, 1)), ("ns2", lambda X: newton_schulz_(A, X, 2)),
                       ("fp64_all", lambda X: refine_fp64_(A, X, all_idx)),
-                      ("df_all", lambda X: refine_df_(A, X, all_idx))):
+                      ("df_all", lambda X: refine_df_(A, X, all_idx)),
+                      ("df_all_with_estimate", lambda X: refine_df_(A, X, all_idx, next_tol=REFINE_TOL))):
         bufs = [(A if label.startswith("inverse") else X0).clone() for _ in range(timing_iters + 2)]
         for b in bufs[:2]:
             fn(b)

@@ -190,3 +190,70 @@ def test_device_flag_list_matches_host_flags(mi_gpu):
     assert set(int(v) for v in lst if v >= 0) == want
     assert all(v in (-1, b) for b, v in enumerate(lst))
     assert 3 in want and set(range(40, 80)) <= want
+
+
+@pytest.mark.gpu
+def test_second_step_estimate(mi_gpu, oracle):
+    """mi_refine_df_next_f32: the step itself is bit-identical to
+    mi_refine_df_f32; a matrix left off the second-step list has error
+    <= tol + 1e-7 (the estimate max|X R^2| / max|X| is first-order, the step
+    adds rounding of about u); skipped and non-finite entries behave; the
+    list may be written over the index array."""
+    import torch
+
+    from matrixinversion_gb300 import refine
+
+    tol = 3e-7
+    A = torch.cat([_inputs(1e3, 64, 51), _inputs(1e5, 448, 52)])
+    X0, _, _ = mi_gpu.batched_inverse(A, "partial")
+    X0[7] = float("nan")
+    batch = A.shape[0]
+    idx = torch.arange(batch, dtype=torch.int32, device="cuda")
+    idx[5] = -1                                           # skipped entries
+    idx[9] = batch + 3
+    X64, _, _ = oracle.inverse_f64(A.cpu().numpy(), "partial")
+
+    Xa = X0.clone()
+    refine.refine_df_(A, Xa, idx)
+    Xb = X0.clone()
+    nxt = refine.refine_df_(A, Xb, idx, next_tol=tol)
+    Xc = X0.clone()
+    lst = idx.clone()
+    same = refine.refine_df_(A, Xc, lst, next_tol=tol, next_out=lst)
+    torch.cuda.synchronize()
+    assert same.data_ptr() == lst.data_ptr()
+    assert torch.equal(Xa.view(torch.int32), Xb.view(torch.int32))
+    assert torch.equal(Xb.view(torch.int32), Xc.view(torch.int32))
+    nx, lc = nxt.cpu().numpy(), lst.cpu().numpy()
+    assert np.array_equal(nx, lc)
+    ix = idx.cpu().numpy()
+    assert nx[5] == -1 and nx[9] == -1 and nx[7] == 7
+    assert all(v in (-1, ix[t]) for t, v in enumerate(nx))
+    x = Xb.cpu().numpy().astype(np.float64)
+    err = np.abs(x - X64).max((1, 2)) / np.abs(X64).max((1, 2))
+    keep = [b for b in range(batch) if b not in (5, 7, 9) and nx[b] == -1]
+    assert len(keep) > batch // 2
+    assert err[keep].max() <= tol + 1e-7, err[keep].max()
+    assert all(nx[b] == -1 for b in range(64) if b != 7)  # kappa = 1e3: one step is enough
+
+
+@pytest.mark.gpu
+def test_refined_inverse_reaches_1e6(mi_gpu, oracle):
+    """The refined form meets max |X - X64| <= 1e-6 max |X64| per matrix in
+    every bucket up to kappa = 1e5, with no second step below kappa = 1e4."""
+    import torch
+
+    from matrixinversion_gb300 import refine
+
+    for kappa, seed in ((3.0, 61), (1e1, 62), (1e3, 63), (1e5, 64)):
+        A = _inputs(kappa, 256, seed)
+        X, perm, info, first, second = refine.refined_inverse(A, lists=True)
+        torch.cuda.synchronize()
+        assert (info.cpu().numpy() == 0).all()
+        X64, _, _ = oracle.inverse_f64(A.cpu().numpy(), "partial")
+        x = X.cpu().numpy().astype(np.float64)
+        err = np.abs(x - X64).max((1, 2)) / np.abs(X64).max((1, 2))
+        assert err.max() <= 1e-6, (kappa, err.max())
+        assert int((first >= 0).sum()) == 256
+        if kappa < 1e4:
+            assert int((second >= 0).sum()) == 0
