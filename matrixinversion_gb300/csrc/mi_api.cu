@@ -115,10 +115,12 @@ PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
 
 template <int N>
 static void geom_of(int& lanes, int& mpw, int& smem_warp) {
-    if constexpr (N <= kTinyMax) {     // one thread per matrix, no shared memory
+    if constexpr (N <= tiny_max_contig<kModeReference>()) {     // one thread per matrix
         lanes = 1;
         mpw = 32;
-        smem_warp = 0;
+        // staged through shared memory unless each thread moves its matrix
+        // with 16-byte copies
+        smem_warp = ((N * N) % 4 == 0 && N <= kTinyMax) ? 0 : 32 * tiny_pitch<N>() * 4;
         return;
     }
     constexpr int L = default_lanes(N, kModeReference);

@@ -573,8 +573,8 @@ __device__ __forceinline__ void set_row(float (&a)[G::R][G::C], int q, const flo
 // rows are permuted at the store (output row of a slot = the step that chose
 // it); the arithmetic of every row is that of the exchanging form.
 template <class G>
-__device__ __forceinline__ void gj_step_partial(float (&a)[G::R][G::C], float (&ps)[G::R], const int k, int rg, int cg,
-                                                int s, int gbase, float* scr, int& lp, bool& placed) {
+__device__ __forceinline__ void gj_step_partial(float (&a)[G::R][G::C], const int k, int rg, int cg, int s, int gbase,
+                                                float* scr, int& lp, bool& placed) {
     constexpr int R = G::R, C = G::C;
     const int kc = k / C, kci = k % C;
     float* cb = scr + G::oCol + (k & 1) * G::kCol;
@@ -602,17 +602,20 @@ __device__ __forceinline__ void gj_step_partial(float (&a)[G::R][G::C], float (&
     } else if (lp == k) {
         lp = (int)lw;
     }
-    const int rr = r % G::RG, rri = r / G::RG;
-    if (rg == rr) {           // slot r's row is the pivot row
-        float w[C];
-        get_row<G>(a, rri, w);
-        sts_vec<C>(rb + cg * C, w);
-    }
+    // slot r's row is the pivot row: its owners store it straight from the
+    // register row that holds it (one predicated store per row, no select)
+    bool piv[R];
+#pragma unroll
+    for (int ri = 0; ri < R; ri++) piv[ri] = (rg + G::RG * ri == r);
+#pragma unroll
+    for (int ri = 0; ri < R; ri++)
+        if (piv[ri]) sts_vec<C>(rb + cg * C, a[ri]);
     __syncwarp();
     float w[C];
     lds_vec<C>(rb + cg * C, w);
-    const float d = cb[rr * R + rri];
+    const float d = cb[(r % G::RG) * R + r / G::RG];
     const float p = recip(d);
+    // pivot value of the step (the row scales are formed from these at the end)
     if (s < G::kN) scr[G::oD + k] = d;    // every lane writes the same value
     if (s == 0) reinterpret_cast<int*>(scr + G::oWin)[k] = r;
     if (cg == kc) w[kci] = 1.0f;
@@ -620,10 +623,8 @@ __device__ __forceinline__ void gj_step_partial(float (&a)[G::R][G::C], float (&
     lds_vec<R>(cb + rg * R, c);
 #pragma unroll
     for (int ri = 0; ri < R; ri++) {
-        const bool piv = (rg + G::RG * ri == r);
-        c[ri] = piv ? 0.0f : c[ri];
-        ps[ri] = piv ? p : ps[ri];
-        if (cg == kc) a[ri][kci] = piv ? 1.0f : 0.0f;
+        c[ri] = piv[ri] ? 0.0f : c[ri];
+        if (cg == kc) a[ri][kci] = piv[ri] ? 1.0f : 0.0f;
     }
 #pragma unroll
     for (int ri = 0; ri < R; ri++) row_update<C>(a[ri], c[ri] * p, w);
@@ -792,10 +793,18 @@ __device__ __forceinline__ void phase_eliminate(float (&a)[GeomN<N, L, MODE>::R]
         int lp = s;
         bool placed = (s >= N);
 #pragma unroll
-        for (int k = 0; k < N; ++k) gj_step_partial<G>(a, ps, k, rg, cg, s, mslot * L, scr, lp, placed);
+        for (int k = 0; k < N; ++k) gj_step_partial<G>(a, k, rg, cg, s, mslot * L, scr, lp, placed);
         __syncwarp();
         // output row of each slot = the step that chose it
         if (s < N) reinterpret_cast<int*>(scr + G::oMap)[reinterpret_cast<const int*>(scr + G::oWin)[s]] = s;
+        __syncwarp();
+        // scale of each row = 1 / the pivot of the step that chose its slot
+        const int* omap = reinterpret_cast<const int*>(scr + G::oMap);
+#pragma unroll
+        for (int ri = 0; ri < R; ri++) {
+            const int slot = rg + G::RG * ri;
+            if (slot < N) ps[ri] = recip(scr[G::oD + omap[slot]]);
+        }
     } else {
 #pragma unroll
         for (int k = 0; k < N; ++k) gj_step<G>(a, ps, k, rg, cg, mslot * L, scr);

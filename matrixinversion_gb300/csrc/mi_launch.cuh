@@ -46,7 +46,7 @@ inline bool make_tensor_map(CUtensorMap* map, float* a, int n, long long batch, 
 template <int N, int MODE>
 cudaError_t launch(float* a, int32_t* perm, int32_t* info, long long batch, int tpb, int grid,
                    cudaStream_t stream) {
-    if constexpr (N <= kTinyMax) return launch_tiny<N, MODE>(a, perm, info, batch, tpb, grid, stream);
+    if constexpr (N <= tiny_max_contig<MODE>()) return launch_tiny<N, MODE>(a, perm, info, batch, tpb, grid, stream);
     constexpr int L = default_lanes(N, MODE);
     using G = Geom<N, L>;
     const int warps = tpb / 32;

@@ -1,6 +1,6 @@
-// mi_tiny.cuh -- n <= 8: one thread per matrix.
+// mi_tiny.cuh -- small n: one thread per matrix.
 //
-// At these sizes a matrix is 4 to 256 bytes, and the lane groups of the
+// At these sizes a matrix is 4 to 784 bytes, and the lane groups of the
 // sub-warp kernel spend more instructions on coordination than on the
 // arithmetic.  Here each thread loads its matrix into registers, evaluates
 // the pivot rule serially (the reference's tree with T = n slots, the
@@ -19,7 +19,15 @@
 
 namespace mi {
 
-constexpr int kTinyMax = 8;
+constexpr int kTinyMax = 8;        // register-only form (and the descriptor-bucket kernel)
+constexpr int kTinySlotMax = 14;   // largest n of the shared-memory-slot form
+
+// Largest n inverted one thread per matrix for contiguous batches, per pivot
+// mode.  Measured on GB300 at 1,000,000 matrices against the sub-warp kernel
+// (same results bit for bit): n = 9 .. 14 run 1.2-3.5x faster in the no-pivot
+// and reference modes and 2.5-7.8x in partial mode.
+template <int MODE>
+__host__ __device__ constexpr int tiny_max_contig() { return 14; }
 
 // |x| with subnormals flushed to zero, NaN kept (compares as false): the
 // reference's fast-math fabs in its pivot compares.
@@ -40,8 +48,8 @@ __device__ __forceinline__ float tiny_get(const float (&a)[N][N], int r, int c) 
 // Pivot sequence of the reference rules on the raw matrix: win[k] = input
 // row placed at step k.  Parallel rule: per slot t, the diagonal against row
 // k+1+t (strict '>'), then the tree with strides T/2 .. 1 (strict '<').
-template <int N, int MODE>
-__device__ __forceinline__ void tiny_pivots(const float (&a)[N][N], int (&win)[N]) {
+template <int N, int MODE, class Get>
+__device__ __forceinline__ void tiny_pivots_by(Get get, int (&win)[N]) {
 #pragma unroll
     for (int i = 0; i < N; i++) win[i] = i;
 #pragma unroll
@@ -50,14 +58,14 @@ __device__ __forceinline__ void tiny_pivots(const float (&a)[N][N], int (&win)[N
         if constexpr (MODE == kModeReference) {
             float vals[N];
             int idxs[N];
-            const float dk = tiny_ref_key(tiny_get<N>(a, win[k], k));
+            const float dk = tiny_ref_key(get(win[k], k));
 #pragma unroll
             for (int t = 0; t < N; t++) {
                 vals[t] = dk;
                 idxs[t] = k;
                 const int i = k + 1 + t;
                 if (i < N) {
-                    const float w = tiny_ref_key(tiny_get<N>(a, win[i], k));
+                    const float w = tiny_ref_key(get(win[i], k));
                     if (w > vals[t]) {
                         vals[t] = w;
                         idxs[t] = i;
@@ -74,10 +82,10 @@ __device__ __forceinline__ void tiny_pivots(const float (&a)[N][N], int (&win)[N
                     }
             p = idxs[0];
         } else {   // serial scan
-            float mv = tiny_ref_key(tiny_get<N>(a, win[k], k));
+            float mv = tiny_ref_key(get(win[k], k));
 #pragma unroll
             for (int i = k + 1; i < N; i++) {
-                const float w = tiny_ref_key(tiny_get<N>(a, win[i], k));
+                const float w = tiny_ref_key(get(win[i], k));
                 if (w > mv) {
                     mv = w;
                     p = i;
@@ -95,6 +103,11 @@ __device__ __forceinline__ void tiny_pivots(const float (&a)[N][N], int (&win)[N
             if (p == i) win[i] = wk;
         win[k] = wp;
     }
+}
+
+template <int N, int MODE>
+__device__ __forceinline__ void tiny_pivots(const float (&a)[N][N], int (&win)[N]) {
+    tiny_pivots_by<N, MODE>([&](int r, int c) { return tiny_get<N>(a, r, c); }, win);
 }
 
 // One Gauss-Jordan step on rows already in pivot order (as gj_step).
@@ -201,6 +214,49 @@ __device__ __forceinline__ void tiny_invert(const float (&a)[N][N], float (&b)[N
         if (dv[k] == 0.0f) info = k + 1;
 }
 
+// n > 8: the matrix is read from and written back to this thread's
+// shared-memory slot (row-major, pitch n), so the rows and columns chosen at
+// run time (pivot order, output permutation) are addressed directly instead
+// of through register select chains, which grow as n^3.  Same arithmetic as
+// tiny_invert.
+template <int N, int MODE>
+__device__ __forceinline__ void tiny_invert_slot(float* sm, int (&win)[N], int& info) {
+    float b[N][N];
+    if constexpr (MODE == kModeReference || MODE == kModeReferenceSerial) {
+        tiny_pivots_by<N, MODE>([&](int r, int c) { return sm[r * N + c]; }, win);
+#pragma unroll
+        for (int i = 0; i < N; i++) {
+            const float* row = sm + win[i] * N;
+#pragma unroll
+            for (int j = 0; j < N; j++) b[i][j] = row[j];
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < N; i++) {
+            win[i] = i;
+#pragma unroll
+            for (int j = 0; j < N; j++) b[i][j] = sm[i * N + j];
+        }
+    }
+    float ps[N], dv[N];
+#pragma unroll
+    for (int k = 0; k < N; k++) {
+        if constexpr (MODE == kModePartial) tiny_step_partial<N>(b, ps, dv, win, k);
+        else tiny_step<N>(b, ps, dv, k);
+    }
+    info = 0;
+#pragma unroll
+    for (int k = N - 1; k >= 0; k--)
+        if (dv[k] == 0.0f) info = k + 1;
+    // A^-1[i][win[j]] = b[i][j] * ps[i]
+#pragma unroll
+    for (int i = 0; i < N; i++) {
+        float* row = sm + i * N;
+#pragma unroll
+        for (int j = 0; j < N; j++) row[win[j]] = b[i][j] * ps[i];
+    }
+}
+
 template <int N>
 __device__ __forceinline__ void tiny_load(const float* src, float (&a)[N][N]) {
     if constexpr ((N * N) % 4 == 0) {
@@ -249,23 +305,28 @@ __device__ __forceinline__ void tiny_store(float* dst, const float (&b)[N][N], c
     for (int e = 0; e < N * N; e++) dst[e] = o[e / N][e % N];
 }
 
-// Contiguous batch, one matrix per thread.  When n * n is a multiple of 4
-// each thread moves its matrix with 16-byte loads and stores (16-byte-aligned
-// batch); otherwise each warp's 32 consecutive matrices move between global
-// and shared memory with coalesced copies and each thread reads and writes
-// its own matrix there at an odd pitch (conflict-free).  Measured on GB300:
-// the staged copies win for n = 3, 5, 7 and lose for n = 2, 4, 6, 8.
-constexpr int kTinyThreads = 128;
+// Contiguous batch, one matrix per thread.  When n <= 8 and n * n is a
+// multiple of 4 each thread moves its matrix with 16-byte loads and stores
+// (16-byte-aligned batch); otherwise each warp's 32 consecutive matrices move
+// between global and shared memory with coalesced copies and each thread
+// reads and writes its own matrix there at an odd pitch (conflict-free).
+// Measured on GB300: the staged copies win for n = 3, 5, 7 and lose for
+// n = 2, 4, 6, 8.  Above n = 8 the slot form always stages (its row and
+// column permutations address the slot).
+template <int N>
+__host__ __device__ constexpr int tiny_warps() { return N <= 8 ? 4 : (N <= 13 ? 2 : 1); }   // static staging <= 48 KB
+template <int N>
+__host__ __device__ constexpr int tiny_threads() { return 32 * tiny_warps<N>(); }
 
 template <int N>
 __host__ __device__ constexpr int tiny_pitch() { return (N * N) | 1; }
 
 template <int N, int MODE>
-__global__ void __launch_bounds__(kTinyThreads) mi_tiny_kernel(float* __restrict__ A, int32_t* __restrict__ perm_out,
-                                                              int32_t* __restrict__ info_out, long long batch,
-                                                              int vec) {
-    constexpr int NN = N * N, P = tiny_pitch<N>();
-    if constexpr (NN % 4 == 0) {
+__global__ void __launch_bounds__(tiny_threads<N>()) mi_tiny_kernel(float* __restrict__ A, int32_t* __restrict__ perm_out,
+                                                                   int32_t* __restrict__ info_out, long long batch,
+                                                                   int vec) {
+    constexpr int NN = N * N, P = tiny_pitch<N>(), W = tiny_warps<N>();
+    if constexpr (NN % 4 == 0 && N <= kTinyMax) {
         for (long long b = (long long)blockIdx.x * blockDim.x + threadIdx.x; b < batch;
              b += (long long)gridDim.x * blockDim.x) {
             float a[N][N], x[N][N];
@@ -286,27 +347,51 @@ __global__ void __launch_bounds__(kTinyThreads) mi_tiny_kernel(float* __restrict
         }
         return;
     }
-    __shared__ float stage[kTinyThreads / 32][32 * P];
+    __shared__ float stage[W][32 * P];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     float* st = stage[warp];
-    const long long wstride = (long long)gridDim.x * (kTinyThreads / 32) * 32;
-    for (long long b0 = ((long long)blockIdx.x * (kTinyThreads / 32) + warp) * 32; b0 < batch; b0 += wstride) {
+    const long long wstride = (long long)gridDim.x * W * 32;
+    for (long long b0 = ((long long)blockIdx.x * W + warp) * 32; b0 < batch; b0 += wstride) {
         const int cnt = (batch - b0 < 32) ? (int)(batch - b0) : 32;
         float* g = A + b0 * NN;
-        for (int e = lane; e < cnt * NN; e += 32) st[(e / NN) * P + (e % NN)] = g[e];
+        if (N > kTinyMax && cnt == 32) {
+            // a full group: every copy in flight at once (element e of the
+            // group goes to slot e / NN at pitch P)
+#pragma unroll
+            for (int q = 0; q < NN; q++) {
+                const int e = lane + 32 * q;
+                cp_async_4(st + e + (P - NN) * (e / NN), g + e, true);
+            }
+            cp_async_commit();
+            cp_async_wait_all();
+        } else {
+            for (int e = lane; e < cnt * NN; e += 32) st[(e / NN) * P + (e % NN)] = g[e];
+        }
         __syncwarp();
         const bool mine = lane < cnt;
-        float a[N][N], x[N][N];
         int win[N], info = 0;
         if (mine) {
             float* sm = st + lane * P;
+            if constexpr (N > kTinyMax) {
+                tiny_invert_slot<N, MODE>(sm, win, info);
+            } else {
+                float a[N][N], x[N][N];
 #pragma unroll
-            for (int e = 0; e < NN; e++) a[e / N][e % N] = sm[e];
-            tiny_invert<N, MODE>(a, x, win, info);
-            tiny_store<N>(sm, x, win, false);
+                for (int e = 0; e < NN; e++) a[e / N][e % N] = sm[e];
+                tiny_invert<N, MODE>(a, x, win, info);
+                tiny_store<N>(sm, x, win, false);
+            }
         }
         __syncwarp();
-        for (int e = lane; e < cnt * NN; e += 32) g[e] = st[(e / NN) * P + (e % NN)];
+        if (N > kTinyMax && cnt == 32) {
+#pragma unroll
+            for (int q = 0; q < NN; q++) {
+                const int e = lane + 32 * q;
+                g[e] = st[e + (P - NN) * (e / NN)];
+            }
+        } else {
+            for (int e = lane; e < cnt * NN; e += 32) g[e] = st[(e / NN) * P + (e % NN)];
+        }
         if (mine) {
             const long long b = b0 + lane;
             if (perm_out != nullptr) {
@@ -349,16 +434,28 @@ __global__ void __launch_bounds__(256) mi_tiny_indexed_kernel(float* __restrict_
 template <int N, int MODE>
 cudaError_t launch_tiny(float* a, int32_t* perm, int32_t* info, long long batch, int /*tpb*/, int grid,
                         cudaStream_t stream) {
+    static_assert(N <= kTinySlotMax, "one thread per matrix up to kTinySlotMax");
     // the block size is fixed by the static staging buffer
+    constexpr int threads = tiny_threads<N>();
     if (grid <= 0) {
-        const long long per_block = kTinyThreads;      // one matrix per thread
+        const long long per_block = threads;           // one matrix per thread
         const long long need = (batch + per_block - 1) / per_block;
-        const long long cap = 16LL * device_sm_count();
+        long long cap = 16LL * device_sm_count();
+        if constexpr (N > kTinyMax) {                   // register bound: as many blocks as are resident
+            static int per_sm = 0;
+            if (per_sm == 0) {
+                cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mi_tiny_kernel<N, MODE>,
+                                                                              threads, 0);
+                if (e != cudaSuccess) return e;
+                if (per_sm < 1) per_sm = 1;
+            }
+            cap = (long long)per_sm * device_sm_count();
+        }
         grid = (int)(need < cap ? need : cap);
     }
     if (grid < 1) grid = 1;
     const int vec = ((N * N) % 4 == 0 && (reinterpret_cast<uintptr_t>(a) & 15u) == 0) ? 1 : 0;
-    mi_tiny_kernel<N, MODE><<<grid, kTinyThreads, 0, stream>>>(a, perm, info, batch, vec);
+    mi_tiny_kernel<N, MODE><<<grid, threads, 0, stream>>>(a, perm, info, batch, vec);
     return cudaGetLastError();
 }
 
