@@ -46,7 +46,11 @@ inline bool make_tensor_map(CUtensorMap* map, float* a, int n, long long batch, 
 template <int N, int MODE>
 cudaError_t launch(float* a, int32_t* perm, int32_t* info, long long batch, int tpb, int grid,
                    cudaStream_t stream) {
-    if constexpr (N <= tiny_max_contig<MODE>()) return launch_tiny<N, MODE>(a, perm, info, batch, tpb, grid, stream);
+    if constexpr (N <= kTinyMax) {
+        return launch_tiny<N, MODE>(a, perm, info, batch, tpb, grid, stream);
+    } else if constexpr (N <= tiny_max_contig<MODE>()) {
+        if (batch >= tiny_min_batch<N, MODE>()) return launch_tiny<N, MODE>(a, perm, info, batch, tpb, grid, stream);
+    }
     constexpr int L = default_lanes(N, MODE);
     using G = Geom<N, L>;
     const int warps = tpb / 32;
@@ -104,7 +108,7 @@ using ilaunch_fn = cudaError_t (*)(float*, const long long*, const int*, const l
 template <int N, int MODE>
 cudaError_t launch_indexed(float* base, const long long* offsets, const int* list, const long long* range,
                            int32_t* perm, int32_t* info, int tpb, int grid, cudaStream_t stream) {
-    if constexpr (N <= kTinyMax)
+    if constexpr (N <= tiny_max_indexed<MODE>())
         return launch_tiny_indexed<N, MODE>(base, offsets, list, range, perm, info, tpb, grid, stream);
     constexpr int L = default_lanes(N, MODE);
     const int warps = tpb / 32;

@@ -20,14 +20,26 @@
 namespace mi {
 
 constexpr int kTinyMax = 8;        // register-only form (and the descriptor-bucket kernel)
-constexpr int kTinySlotMax = 14;   // largest n of the shared-memory-slot form
+constexpr int kTinySlotMax = 15;   // largest n of the shared-memory-slot form (n = 16 spills)
 
 // Largest n inverted one thread per matrix for contiguous batches, per pivot
 // mode.  Measured on GB300 at 1,000,000 matrices against the sub-warp kernel
-// (same results bit for bit): n = 9 .. 14 run 1.2-3.5x faster in the no-pivot
-// and reference modes and 2.5-7.8x in partial mode.
+// (same results bit for bit): n = 9 .. 15 run 1.07-3.5x faster in the
+// no-pivot and reference modes and 1.3-7.8x in partial mode; at n = 16 the
+// 256-value matrix no longer fits in registers and the slot form is 1.4-2x
+// slower.
 template <int MODE>
-__host__ __device__ constexpr int tiny_max_contig() { return 14; }
+__host__ __device__ constexpr int tiny_max_contig() { return 15; }
+
+// Smallest batch for which one thread per matrix beats the lane groups: a
+// small batch leaves few warps per SM, each running one long serial chain.
+// Measured crossovers (n = 12 and 15): 8,192 -> 16,384 matrices without
+// pivoting and with the reference rule, 2,048 -> 8,192 in partial mode; at
+// n = 9 one thread per matrix wins from 2,048 up.
+template <int N, int MODE>
+__host__ __device__ constexpr long long tiny_min_batch() {
+    return (N <= kTinyMax || N <= 10) ? 0 : (MODE == kModePartial ? 4096 : 12288);
+}
 
 // |x| with subnormals flushed to zero, NaN kept (compares as false): the
 // reference's fast-math fabs in its pivot compares.
@@ -431,6 +443,63 @@ __global__ void __launch_bounds__(256) mi_tiny_indexed_kernel(float* __restrict_
     }
 }
 
+// Descriptor bucket, n > 8: each warp takes 32 list entries; the matrices
+// arrive one after another as coalesced 4-byte copies of their n * n floats
+// into the slots (pitch P), every copy in flight before the wait, and leave
+// the same way after each thread has inverted its slot.
+template <int N, int MODE>
+__global__ void __launch_bounds__(tiny_threads<N>()) mi_tiny_slot_indexed_kernel(float* __restrict__ base,
+                                                                                const long long* __restrict__ offsets,
+                                                                                const int* __restrict__ list,
+                                                                                const long long* __restrict__ range,
+                                                                                int32_t* __restrict__ perm_out,
+                                                                                int32_t* __restrict__ info_out) {
+    constexpr int NN = N * N, P = tiny_pitch<N>(), W = tiny_warps<N>();
+    constexpr int Q = (NN + 31) / 32;                   // copies per lane per matrix
+    __shared__ float stage[W][32 * P];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    float* st = stage[warp];
+    const long long start = range[0], count = range[1];
+    const long long wstride = (long long)gridDim.x * W * 32;
+    for (long long t0 = ((long long)blockIdx.x * W + warp) * 32; t0 < count; t0 += wstride) {
+        const long long t = t0 + lane;
+        const bool mine = t < count;
+        const int idx = mine ? list[start + t] : 0;
+        const long long off = mine ? offsets[idx] : 0;
+        const int cnt = (count - t0 < 32) ? (int)(count - t0) : 32;
+        for (int m = 0; m < cnt; m++) {
+            const float* src = base + __shfl_sync(kFull, off, m);
+#pragma unroll
+            for (int q = 0; q < Q; q++) {
+                const int e = lane + 32 * q;
+                if (e < NN) cp_async_4(st + m * P + e, src + e, true);
+            }
+        }
+        cp_async_commit();
+        cp_async_wait_all();
+        __syncwarp();
+        int win[N], info = 0;
+        if (mine) tiny_invert_slot<N, MODE>(st + lane * P, win, info);
+        __syncwarp();
+        for (int m = 0; m < cnt; m++) {
+            float* dst = base + __shfl_sync(kFull, off, m);
+#pragma unroll
+            for (int q = 0; q < Q; q++) {
+                const int e = lane + 32 * q;
+                if (e < NN) dst[e] = st[m * P + e];
+            }
+        }
+        if (mine) {
+            if (perm_out != nullptr) {
+#pragma unroll
+                for (int i = 0; i < N; i++) perm_out[(long long)idx * 32 + i] = win[i];
+            }
+            if (info_out != nullptr) info_out[idx] = info;
+        }
+        __syncwarp();
+    }
+}
+
 template <int N, int MODE>
 cudaError_t launch_tiny(float* a, int32_t* perm, int32_t* info, long long batch, int /*tpb*/, int grid,
                         cudaStream_t stream) {
@@ -462,9 +531,34 @@ cudaError_t launch_tiny(float* a, int32_t* perm, int32_t* info, long long batch,
 template <int N, int MODE>
 cudaError_t launch_tiny_indexed(float* base, const long long* offsets, const int* list, const long long* range,
                                 int32_t* perm, int32_t* info, int tpb, int grid, cudaStream_t stream) {
-    if (grid <= 0) grid = 16 * device_sm_count();
-    mi_tiny_indexed_kernel<N, MODE><<<grid, tpb, 0, stream>>>(base, offsets, list, range, perm, info);
-    return cudaGetLastError();
+    if constexpr (N > kTinyMax) {
+        static_assert(N <= kTinySlotMax, "one thread per matrix up to kTinySlotMax");
+        // persistent warps, as many blocks as are resident (the bucket size is
+        // known only on the device)
+        constexpr int threads = tiny_threads<N>();
+        if (grid <= 0) {
+            static int per_sm = 0;
+            if (per_sm == 0) {
+                cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                    &per_sm, mi_tiny_slot_indexed_kernel<N, MODE>, threads, 0);
+                if (e != cudaSuccess) return e;
+                if (per_sm < 1) per_sm = 1;
+            }
+            grid = per_sm * device_sm_count();
+        }
+        mi_tiny_slot_indexed_kernel<N, MODE><<<grid, threads, 0, stream>>>(base, offsets, list, range, perm, info);
+        return cudaGetLastError();
+    } else {
+        if (grid <= 0) grid = 16 * device_sm_count();
+        mi_tiny_indexed_kernel<N, MODE><<<grid, tpb, 0, stream>>>(base, offsets, list, range, perm, info);
+        return cudaGetLastError();
+    }
 }
+
+// Largest n of a descriptor bucket inverted one thread per matrix (measured:
+// 1,000,000 mixed matrices, n ~ U{2..32}, graph-captured call 2.03 -> 1.98 ms
+// with the slot form for n = 9..15; same bits as the contiguous call).
+template <int MODE>
+__host__ __device__ constexpr int tiny_max_indexed() { return 15; }
 
 }  // namespace mi

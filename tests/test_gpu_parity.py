@@ -261,3 +261,26 @@ def test_copy_paths_keep_neighbours_and_agree(mi_gpu, oracle, n, mode):
             assert np.all(oracle.residual(A, X)[:, 0] <= bound)
         else:
             assert np.all(oracle.residual(A, X)[:, 0] < 1e-5)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n", [11, 12, 15])
+@pytest.mark.parametrize("mode", ["none", "reference", "partial"])
+def test_small_and_large_batch_forms_agree(mi_gpu, n, mode):
+    """n = 11..15 run the lane-group kernel below a batch of 12,288 matrices
+    (4,096 in partial mode) and one thread per matrix above it; the same
+    matrices give the same bits, pivots and info either way."""
+    import torch
+
+    g = torch.Generator(device="cuda").manual_seed(100 + n)
+    big = torch.rand(20000, n, n, generator=g, device="cuda") * 2 - 1
+    if mode == "none":
+        big += n * torch.eye(n, device="cuda")
+    big[5] = 0.0                                          # singular
+    small = big[:2000].clone()
+    Xb, Pb, Ib = mi_gpu.batched_inverse(big, mode)
+    Xs, Ps, Is = mi_gpu.batched_inverse(small, mode)
+    torch.cuda.synchronize()
+    assert torch.equal(Xb[:2000].view(torch.int32), Xs.view(torch.int32))
+    assert torch.equal(Pb[:2000], Ps) and torch.equal(Ib[:2000], Is)
+    assert int(Is[5]) != 0
