@@ -120,7 +120,7 @@ static void geom_of(int& lanes, int& mpw, int& smem_warp) {
         mpw = 32;
         // staged through shared memory unless each thread moves its matrix
         // with 16-byte copies
-        smem_warp = ((N * N) % 4 == 0 && N <= kTinyMax) ? 0 : 32 * tiny_pitch<N>() * 4;
+        smem_warp = ((N * N) % 4 == 0 && N < kTinySlotMin) ? 0 : 32 * tiny_pitch<N>() * 4;
         return;
     }
     constexpr int L = default_lanes(N, kModeReference);

@@ -19,15 +19,19 @@
 
 namespace mi {
 
-constexpr int kTinyMax = 8;        // register-only form (and the descriptor-bucket kernel)
+constexpr int kTinyMax = 8;        // one thread per matrix at any batch size
+constexpr int kTinySlotMin = 3;    // smallest n of the shared-memory-slot form, contiguous batches
 constexpr int kTinySlotMax = 15;   // largest n of the shared-memory-slot form (n = 16 spills)
+constexpr int kTinySlotMinIndexed = 3;   // smallest n of the slot form, descriptor buckets (measured: the uneven call 1.98 -> 1.90 ms against 9)
 
 // Largest n inverted one thread per matrix for contiguous batches, per pivot
 // mode.  Measured on GB300 at 1,000,000 matrices against the sub-warp kernel
 // (same results bit for bit): n = 9 .. 15 run 1.07-3.5x faster in the
 // no-pivot and reference modes and 1.3-7.8x in partial mode; at n = 16 the
 // 256-value matrix no longer fits in registers and the slot form is 1.4-2x
-// slower.
+// slower.  Against the register form (select chains for the row order and
+// the column permutation) the slot form is 1.1-1.8x faster at n = 3..8 and
+// slower only at n = 2.
 template <int MODE>
 __host__ __device__ constexpr int tiny_max_contig() { return 15; }
 
@@ -38,7 +42,7 @@ __host__ __device__ constexpr int tiny_max_contig() { return 15; }
 // n = 9 one thread per matrix wins from 2,048 up.
 template <int N, int MODE>
 __host__ __device__ constexpr long long tiny_min_batch() {
-    return (N <= kTinyMax || N <= 10) ? 0 : (MODE == kModePartial ? 4096 : 12288);
+    return N <= 10 ? 0 : (MODE == kModePartial ? 4096 : 12288);
 }
 
 // |x| with subnormals flushed to zero, NaN kept (compares as false): the
@@ -317,14 +321,13 @@ __device__ __forceinline__ void tiny_store(float* dst, const float (&b)[N][N], c
     for (int e = 0; e < N * N; e++) dst[e] = o[e / N][e % N];
 }
 
-// Contiguous batch, one matrix per thread.  When n <= 8 and n * n is a
-// multiple of 4 each thread moves its matrix with 16-byte loads and stores
-// (16-byte-aligned batch); otherwise each warp's 32 consecutive matrices move
-// between global and shared memory with coalesced copies and each thread
-// reads and writes its own matrix there at an odd pitch (conflict-free).
-// Measured on GB300: the staged copies win for n = 3, 5, 7 and lose for
-// n = 2, 4, 6, 8.  Above n = 8 the slot form always stages (its row and
-// column permutations address the slot).
+// Contiguous batch, one matrix per thread.  n = 2: each thread moves its
+// matrix with 16-byte loads and stores (16-byte-aligned batch) and inverts it
+// in registers.  n = 1 and n >= kTinySlotMin: each warp's 32 consecutive
+// matrices move between global and shared memory with coalesced copies and
+// each thread works on its own matrix there at an odd pitch (conflict-free);
+// from n = 3 up that slot is also where the row order and the column
+// permutation are addressed (tiny_invert_slot).
 template <int N>
 __host__ __device__ constexpr int tiny_warps() { return N <= 8 ? 4 : (N <= 13 ? 2 : 1); }   // static staging <= 48 KB
 template <int N>
@@ -338,7 +341,7 @@ __global__ void __launch_bounds__(tiny_threads<N>()) mi_tiny_kernel(float* __res
                                                                    int32_t* __restrict__ info_out, long long batch,
                                                                    int vec) {
     constexpr int NN = N * N, P = tiny_pitch<N>(), W = tiny_warps<N>();
-    if constexpr (NN % 4 == 0 && N <= kTinyMax) {
+    if constexpr (NN % 4 == 0 && N < kTinySlotMin) {
         for (long long b = (long long)blockIdx.x * blockDim.x + threadIdx.x; b < batch;
              b += (long long)gridDim.x * blockDim.x) {
             float a[N][N], x[N][N];
@@ -366,7 +369,7 @@ __global__ void __launch_bounds__(tiny_threads<N>()) mi_tiny_kernel(float* __res
     for (long long b0 = ((long long)blockIdx.x * W + warp) * 32; b0 < batch; b0 += wstride) {
         const int cnt = (batch - b0 < 32) ? (int)(batch - b0) : 32;
         float* g = A + b0 * NN;
-        if (N > kTinyMax && cnt == 32) {
+        if (N >= kTinySlotMin && cnt == 32) {
             // a full group: every copy in flight at once (element e of the
             // group goes to slot e / NN at pitch P)
 #pragma unroll
@@ -384,7 +387,7 @@ __global__ void __launch_bounds__(tiny_threads<N>()) mi_tiny_kernel(float* __res
         int win[N], info = 0;
         if (mine) {
             float* sm = st + lane * P;
-            if constexpr (N > kTinyMax) {
+            if constexpr (N >= kTinySlotMin) {
                 tiny_invert_slot<N, MODE>(sm, win, info);
             } else {
                 float a[N][N], x[N][N];
@@ -395,7 +398,7 @@ __global__ void __launch_bounds__(tiny_threads<N>()) mi_tiny_kernel(float* __res
             }
         }
         __syncwarp();
-        if (N > kTinyMax && cnt == 32) {
+        if (N >= kTinySlotMin && cnt == 32) {
 #pragma unroll
             for (int q = 0; q < NN; q++) {
                 const int e = lane + 32 * q;
@@ -510,7 +513,7 @@ cudaError_t launch_tiny(float* a, int32_t* perm, int32_t* info, long long batch,
         const long long per_block = threads;           // one matrix per thread
         const long long need = (batch + per_block - 1) / per_block;
         long long cap = 16LL * device_sm_count();
-        if constexpr (N > kTinyMax) {                   // register bound: as many blocks as are resident
+        if constexpr (N >= kTinySlotMin) {              // as many blocks as are resident
             static int per_sm = 0;
             if (per_sm == 0) {
                 cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mi_tiny_kernel<N, MODE>,
@@ -531,7 +534,7 @@ cudaError_t launch_tiny(float* a, int32_t* perm, int32_t* info, long long batch,
 template <int N, int MODE>
 cudaError_t launch_tiny_indexed(float* base, const long long* offsets, const int* list, const long long* range,
                                 int32_t* perm, int32_t* info, int tpb, int grid, cudaStream_t stream) {
-    if constexpr (N > kTinyMax) {
+    if constexpr (N >= kTinySlotMinIndexed) {
         static_assert(N <= kTinySlotMax, "one thread per matrix up to kTinySlotMax");
         // persistent warps, as many blocks as are resident (the bucket size is
         // known only on the device)
