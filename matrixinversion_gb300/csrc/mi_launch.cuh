@@ -24,6 +24,7 @@ PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder();  // driver entry point (
 }  // namespace mi
 
 #include "mi_tiny.cuh"
+#include "mi_rows.cuh"
 
 namespace mi {
 
@@ -51,6 +52,8 @@ cudaError_t launch(float* a, int32_t* perm, int32_t* info, long long batch, int 
     } else if constexpr (N <= tiny_max_contig<MODE>()) {
         if (batch >= tiny_min_batch<N, MODE>()) return launch_tiny<N, MODE>(a, perm, info, batch, tpb, grid, stream);
     }
+    if constexpr (MODE == kModePartial && N >= kRowsMin && rows_partial_enabled<N>())
+        return launch_rows_partial<N>(a, perm, info, batch, grid, stream);
     constexpr int L = default_lanes(N, MODE);
     using G = Geom<N, L>;
     const int warps = tpb / 32;

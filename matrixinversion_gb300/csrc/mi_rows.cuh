@@ -1,0 +1,326 @@
+// mi_rows.cuh -- partial pivoting for n = 16..32 with whole rows per lane.
+//
+// 16 lanes per matrix, two matrices per warp; lane s of a group owns the
+// rows (slots) s and s + 16 in registers, every column of them.  A step of
+// partial pivoting then needs no exchange of column values between lanes:
+// each lane keys column k of its own rows, one 16-lane maximum over a packed
+// (key, logical row, slot) word picks getrf's pivot (largest |x|, ties to the
+// lowest logical row), the winning lane stores its row to a small
+// shared-memory buffer and every lane reads it back as broadcast 16-byte
+// loads.  Rows stay in their slots (no exchanges); as in gj_step_partial each
+// slot carries its logical position, the output row of a slot is the step
+// that chose it, and the columns leave through the pivot permutation.  The
+// arithmetic of every element (m = c * (1/pivot), a = fma(-m, w, a), column k
+// zeroed first with w[k] = 1, rows scaled by 1/pivot at the end) is that of
+// gj_step_partial, so the results are the same bits.
+//
+// The warp's two matrices move between HBM and a padded shared-memory stage
+// (row pitch an odd number of 16-byte chunks: conflict-free row reads) with
+// asynchronous copies, 16 bytes at a time when rows allow.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "mi_kernel.cuh"
+
+namespace mi {
+
+constexpr int kRowsLanes = 16;      // lanes per matrix
+constexpr int kRowsMats = 2;        // matrices per warp
+constexpr int kRowsWarps = 4;       // warps per block (3 blocks per SM at up to 170 registers)
+constexpr int kRowsMin = 16;        // smallest n of this kernel (partial pivoting)
+
+template <int N>
+struct RowsGeom {
+    static_assert(N >= 1 && N <= 32, "n must be in 1..32");
+    static constexpr int R = (N + kRowsLanes - 1) / kRowsLanes;     // rows per lane
+    static constexpr int NC = (N + 3) & ~3;                         // register columns
+    static constexpr int SP = (((N + 3) / 4) | 1) * 4;              // stage row pitch (floats)
+    static constexpr int kMat = N * SP;                             // stage floats per matrix
+    // per-matrix scratch (floats): two pivot-row buffers, pivots, pivot slots,
+    // output row of each slot
+    static constexpr int oRow = 0;
+    static constexpr int oD = oRow + 2 * NC;
+    static constexpr int oWin = oD + 32;
+    static constexpr int oMap = oWin + 32;
+    static constexpr int kScr = oMap + 32;
+    static constexpr int oScr = kRowsMats * kMat;                   // scratch after the stage
+    static constexpr int kWarp = (oScr + kRowsMats * kScr + 31) & ~31;   // floats per warp (128-byte multiple)
+    static_assert(kMat % 4 == 0 && kScr % 4 == 0 && NC % 4 == 0, "16-byte alignment of rows and buffers");
+};
+
+__device__ __forceinline__ void cp_async_16(float* dst, const float* src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_addr(dst)), "l"(src) : "memory");
+}
+
+// Partial-pivoting key of one entry: |x| bits + 2 (a NaN never beats a
+// number: key 1), as gj_step_partial.
+__device__ __forceinline__ unsigned rows_key(float x) {
+    const unsigned b = __float_as_uint(x) & 0x7fffffffu;
+    return (b > 0x7f800000u) ? 1u : b + 2u;
+}
+
+// Maximum over the 16 lanes of this lane's group (xor offsets < 16 stay in
+// the group).  Measured: one redux.sync per group mask instead (both groups
+// of a warp in one instruction) is 6-10% slower here.
+__device__ __forceinline__ unsigned rows_group_max(unsigned v) {
+#pragma unroll
+    for (int o = 8; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(kFull, v, o));
+    return v;
+}
+
+template <int N>
+__global__ void __launch_bounds__(32 * kRowsWarps, 3) mi_rows_partial_kernel(float* __restrict__ A,
+                                                                            int32_t* __restrict__ perm_out,
+                                                                            int32_t* __restrict__ info_out,
+                                                                            long long batch, int vec) {
+    using G = RowsGeom<N>;
+    constexpr int R = G::R, NC = G::NC, SP = G::SP, NN = N * N;
+    extern __shared__ float4 rows_smem[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    float* ws = reinterpret_cast<float*>(rows_smem) + warp * G::kWarp;
+    const int mslot = lane >> 4, s = lane & 15, gbase = mslot * kRowsLanes;
+    float* st = ws + mslot * G::kMat;                    // this lane's matrix in the stage
+    float* scr = ws + G::oScr + mslot * G::kScr;
+    int* win = reinterpret_cast<int*>(scr + G::oWin);
+    int* omap = reinterpret_cast<int*>(scr + G::oMap);
+    const long long groups = (batch + kRowsMats - 1) / kRowsMats;
+    const long long wstride = (long long)gridDim.x * kRowsWarps;
+    for (long long grp = (long long)blockIdx.x * kRowsWarps + warp; grp < groups; grp += wstride) {
+        const long long b0 = grp * kRowsMats;
+        const int cnt = (batch - b0 < kRowsMats) ? (int)(batch - b0) : kRowsMats;
+        float* g = A + b0 * NN;
+        // ---- in: the group's cnt * n * n floats into the padded stage
+        if (vec) {                                       // n % 4 == 0, 16-byte-aligned batch
+            constexpr int Q4 = (N / 4 > 0) ? N / 4 : 1;  // chunks per row
+            const int total = cnt * (NN / 4);
+#pragma unroll 4
+            for (int c = lane; c < total; c += 32) {
+                const int m = c / (NN / 4), rem = c - m * (NN / 4);
+                const int row = rem / Q4, c4 = rem - row * Q4;
+                cp_async_16(ws + m * G::kMat + row * SP + 4 * c4, g + 4 * c);
+            }
+        } else {
+            const int total = cnt * NN;
+#pragma unroll 4
+            for (int e = lane; e < total; e += 32) {
+                const int m = e / NN, rem = e - m * NN;
+                const int row = rem / N, col = rem - row * N;
+                cp_async_4(ws + m * G::kMat + row * SP + col, g + e, true);
+            }
+        }
+        cp_async_commit();
+        cp_async_wait_all();
+        __syncwarp();
+        const bool valid = mslot < cnt;
+        // ---- my rows to registers (padding rows and columns are zero)
+        float a[R][NC];
+#pragma unroll
+        for (int ri = 0; ri < R; ri++) {
+            const int slot = s + kRowsLanes * ri;
+            const bool in = valid && slot < N;
+#pragma unroll
+            for (int q = 0; q < NC / 4; q++) {
+                float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (in) v = *reinterpret_cast<const float4*>(st + slot * SP + 4 * q);
+                a[ri][4 * q] = v.x;
+                a[ri][4 * q + 1] = v.y;
+                a[ri][4 * q + 2] = v.z;
+                a[ri][4 * q + 3] = v.w;
+            }
+#pragma unroll
+            for (int j = N; j < NC; j++) a[ri][j] = 0.0f;
+        }
+        // ---- n steps of partial pivoting
+        int lp[R];
+        bool placed[R];
+#pragma unroll
+        for (int ri = 0; ri < R; ri++) {
+            lp[ri] = s + kRowsLanes * ri;
+            placed[ri] = (s + kRowsLanes * ri >= N);
+        }
+#pragma unroll
+        for (int k = 0; k < N; k++) {
+            // my candidate: the largest key, then the lowest logical row
+            unsigned bk = 0u;
+            int bl = 255, bs = 0;
+#pragma unroll
+            for (int ri = 0; ri < R; ri++) {
+                const unsigned key = placed[ri] ? 0u : rows_key(a[ri][k]);
+                if (key > bk || (key == bk && key != 0u && lp[ri] < bl)) {
+                    bk = key;
+                    bl = lp[ri];
+                    bs = s + kRowsLanes * ri;
+                }
+            }
+            const unsigned mx = rows_group_max(bk);
+            const unsigned cand = (bk != 0u && bk == mx) ? (((unsigned)(255 - bl) << 8) | (unsigned)bs) : 0u;
+            const unsigned best = rows_group_max(cand);
+            const int r = (int)(best & 0xffu);               // pivot slot
+            const int lw = 255 - (int)(best >> 8);           // its logical row
+#pragma unroll
+            for (int ri = 0; ri < R; ri++) {
+                if (s + kRowsLanes * ri == r) {
+                    lp[ri] = k;
+                    placed[ri] = true;
+                } else if (lp[ri] == k) {
+                    lp[ri] = lw;                             // the row at logical k takes the winner's place
+                }
+            }
+            // the pivot row, from its owner through a double-buffered row buffer
+            float* rb = scr + G::oRow + (k & 1) * NC;
+#pragma unroll
+            for (int ri = 0; ri < R; ri++)
+                if (s + kRowsLanes * ri == r) {
+#pragma unroll
+                    for (int q = 0; q < NC / 4; q++)
+                        *reinterpret_cast<float4*>(rb + 4 * q) =
+                            make_float4(a[ri][4 * q], a[ri][4 * q + 1], a[ri][4 * q + 2], a[ri][4 * q + 3]);
+                }
+            __syncwarp();
+            const float d = rb[k];
+            const float p = recip(d);
+            if (s == 0) {
+                scr[G::oD + k] = d;
+                win[k] = r;
+            }
+            float2 nm[R];
+#pragma unroll
+            for (int ri = 0; ri < R; ri++) {
+                const bool piv = (s + kRowsLanes * ri == r);
+                const float c = piv ? 0.0f : a[ri][k];       // the pivot row takes no update
+                a[ri][k] = piv ? 1.0f : 0.0f;                // column k becomes -multiplier (w[k] = 1)
+                const float m = c * p;
+                nm[ri] = make_float2(-m, -m);
+            }
+            // the pivot row streams through in 16-byte chunks (4 values live)
+#pragma unroll
+            for (int q = 0; q < NC / 4; q++) {
+                float4 v = *reinterpret_cast<const float4*>(rb + 4 * q);
+                if (k == 4 * q) v.x = 1.0f;
+                if (k == 4 * q + 1) v.y = 1.0f;
+                if (k == 4 * q + 2) v.z = 1.0f;
+                if (k == 4 * q + 3) v.w = 1.0f;
+#pragma unroll
+                for (int ri = 0; ri < R; ri++) {
+                    float2 x0 = make_float2(a[ri][4 * q], a[ri][4 * q + 1]);
+                    float2 x1 = make_float2(a[ri][4 * q + 2], a[ri][4 * q + 3]);
+                    x0 = __ffma2_rn(nm[ri], make_float2(v.x, v.y), x0);
+                    x1 = __ffma2_rn(nm[ri], make_float2(v.z, v.w), x1);
+                    a[ri][4 * q] = x0.x;
+                    a[ri][4 * q + 1] = x0.y;
+                    a[ri][4 * q + 2] = x1.x;
+                    a[ri][4 * q + 3] = x1.y;
+                }
+            }
+        }
+        __syncwarp();
+        // output row of each slot = the step that chose it; row scale = 1 / its pivot
+#pragma unroll
+        for (int ri = 0; ri < R; ri++) {
+            const int t = s + kRowsLanes * ri;
+            if (t < N) omap[win[t]] = t;
+        }
+        __syncwarp();
+#pragma unroll
+        for (int ri = 0; ri < R; ri++) {
+            const int slot = s + kRowsLanes * ri;
+            const float ps = (slot < N) ? recip(scr[G::oD + omap[slot]]) : 1.0f;
+#pragma unroll
+            for (int q = 0; q < NC / 2; q++) {
+                const float2 x = __fmul2_rn(make_float2(a[ri][2 * q], a[ri][2 * q + 1]), make_float2(ps, ps));
+                a[ri][2 * q] = x.x;
+                a[ri][2 * q + 1] = x.y;
+            }
+        }
+        // ---- rows to the stage in output order, columns through the pivot
+        // permutation: A^-1[omap[slot]][win[j]] = X[slot][j]
+        if (valid) {
+#pragma unroll
+            for (int ri = 0; ri < R; ri++) {
+                const int slot = s + kRowsLanes * ri;
+                if (slot < N) {
+                    float* orow = st + omap[slot] * SP;
+#pragma unroll
+                    for (int j = 0; j < N; j++) orow[win[j]] = a[ri][j];
+                }
+            }
+        }
+        __syncwarp();
+        // ---- out
+        if (vec) {
+            constexpr int Q4 = (N / 4 > 0) ? N / 4 : 1;
+            const int total = cnt * (NN / 4);
+#pragma unroll 4
+            for (int c = lane; c < total; c += 32) {
+                const int m = c / (NN / 4), rem = c - m * (NN / 4);
+                const int row = rem / Q4, c4 = rem - row * Q4;
+                *reinterpret_cast<float4*>(g + 4 * c) =
+                    *reinterpret_cast<const float4*>(ws + m * G::kMat + row * SP + 4 * c4);
+            }
+        } else {
+            const int total = cnt * NN;
+#pragma unroll 4
+            for (int e = lane; e < total; e += 32) {
+                const int m = e / NN, rem = e - m * NN;
+                const int row = rem / N, col = rem - row * N;
+                g[e] = ws[m * G::kMat + row * SP + col];
+            }
+        }
+        // ---- pivots and info (first exactly-zero pivot, 1-based)
+        unsigned zmask = 0u;
+#pragma unroll
+        for (int ri = 0; ri < R; ri++) {
+            const int t = s + kRowsLanes * ri;
+            const bool z = valid && t < N && scr[G::oD + t] == 0.0f;
+            zmask |= ((__ballot_sync(kFull, z) >> gbase) & 0xffffu) << (kRowsLanes * ri);
+            if (valid && t < N && perm_out != nullptr) perm_out[(b0 + mslot) * N + t] = win[t];
+        }
+        if (valid && s == 0 && info_out != nullptr) info_out[b0 + mslot] = zmask ? __ffs(zmask) : 0;
+        __syncwarp();
+    }
+}
+
+// Launch over a contiguous batch: persistent warps, as many blocks as are
+// resident.
+template <int N>
+cudaError_t launch_rows_partial(float* a, int32_t* perm, int32_t* info, long long batch, int grid,
+                                cudaStream_t stream) {
+    using G = RowsGeom<N>;
+    constexpr int threads = 32 * kRowsWarps;
+    constexpr size_t smem = (size_t)kRowsWarps * G::kWarp * sizeof(float);
+    auto kern = mi_rows_partial_kernel<N>;
+    static int per_sm = 0;
+    if (per_sm == 0) {
+        if (smem > 48 * 1024) {
+            cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e != cudaSuccess) return e;
+        }
+        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem);
+        if (e != cudaSuccess) return e;
+        if (per_sm < 1) per_sm = 1;
+    }
+    const long long groups = (batch + kRowsMats - 1) / kRowsMats;
+    if (grid <= 0) {
+        const long long need = (groups + kRowsWarps - 1) / kRowsWarps;
+        const long long cap = (long long)per_sm * device_sm_count();
+        grid = (int)(need < cap ? need : cap);
+    }
+    if (grid < 1) grid = 1;
+    const int vec = (N % 4 == 0 && (reinterpret_cast<uintptr_t>(a) & 15u) == 0) ? 1 : 0;
+    kern<<<grid, threads, smem, stream>>>(a, perm, info, batch, vec);
+    return cudaGetLastError();
+}
+
+// Whether partial pivoting at size n uses this kernel (contiguous batches).
+// Measured on GB300 at 1,000,000 matrices against the lane-block kernel
+// (gj_step_partial, one matrix per warp above n = 16), same bits: n = 16
+// 1.63 -> 1.20 ms, 17 3.68 -> 2.59, 20 4.20 -> 2.65, 24 4.99 -> 4.21, 28
+// 6.33 -> 5.27, 32 6.99 -> 6.76; at n = 29..31 this kernel spills registers
+// and n = 31 was 5% slower.
+template <int N>
+__host__ __device__ constexpr bool rows_partial_enabled() { return N <= 28 || N == 32; }
+
+}  // namespace mi
