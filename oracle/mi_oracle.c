@@ -2,7 +2,8 @@
  * mi_oracle.c -- CPU restatement of the reference's batched LU-inverse path.
  *
  * TEST INFRASTRUCTURE ONLY.  This file is the oracle: the parity tests, the
- * smoke check and the CPU-baseline leg of the benchmark link it as the checker.
+ * smoke check and the CPU-baseline leg of the benchmark link it to check (or,
+ * for the baseline, time) the CUDA path against it.
  * The product path (matrixinversion_gb300 + its CUDA library) never calls it.
  *
  * What it restates (paths are relative to the reference project root):
