@@ -76,19 +76,48 @@ int mi_inverse_f32(float* d_a, int32_t* d_perm, int32_t* d_info, int64_t batch, 
 /*
  * As mi_inverse_f32 with explicit launch knobs.
  *   threads_per_block  the NUMTHREADS knob; rounded up to a multiple of 32 and
- *                      capped at 256; 0 = default.
+ *                      capped at 256; 0 = default.  Used by the lane-group
+ *                      kernel form only (mi_query_launch says which form a
+ *                      call runs); the other forms have a fixed block.
  *   grid_blocks        0 = sized from the device's SM count and occupancy.
  */
 int mi_inverse_cfg_f32(float* d_a, int32_t* d_perm, int32_t* d_info, int64_t batch, int n, int pivot,
                        int threads_per_block, int grid_blocks, void* stream);
 
 /*
- * Launch geometry for size n: lanes per matrix, matrices per warp, shared
- * memory bytes per warp, and the default threads per block.  Any out pointer
- * may be NULL.  Needs no GPU.
+ * Launch geometry for size n without pivoting or with the reference rules on
+ * large batches: lanes per matrix, matrices per warp, shared memory bytes per
+ * warp, and the default threads per block.  Any out pointer may be NULL.
+ * Needs no GPU.  mi_query_launch gives the geometry for any pivot mode and
+ * batch size.
  */
 int mi_query_config(int n, int* lanes_per_matrix, int* matrices_per_warp, int* smem_bytes_per_warp,
                     int* default_threads_per_block);
+
+/*
+ * Kernel forms of a contiguous call (mi_query_launch).  Only the lane-group
+ * form launches with the NUMTHREADS knob (threads_per_block of
+ * mi_inverse_cfg_f32, or the installed mi_set_launch_config entry); the other
+ * two have a fixed block, and the knob changes nothing there.
+ */
+#define MI_FORM_THREAD 1 /* one thread per matrix (n <= 8; n = 9..15 on large batches)  */
+#define MI_FORM_LANES 2  /* a group of lanes per matrix, register blocks              */
+#define MI_FORM_ROWS 3   /* 16 lanes per matrix, whole rows per lane (partial pivoting) */
+
+/*
+ * The kernel a contiguous mi_inverse_cfg_f32(..., batch, n, pivot,
+ * threads_per_block, ...) call launches (no counterpart in the reference,
+ * whose launch geometry is its compile-time template arguments,
+ * parallel_pivot/luBatchedInplace.cu:4-11): *form (MI_FORM_*), lanes per
+ * matrix, matrices per warp, and the threads per block it launches with --
+ * threads_per_block resolved as that call resolves it (0 = the installed
+ * entry; rounded up to a multiple of 32, capped at 256) for MI_FORM_LANES,
+ * the form's fixed block otherwise.  Any out pointer may be NULL.  Needs no
+ * GPU.  Descriptor buckets (mi_inverse_descr_f32) choose their kernels per
+ * bucket and are not covered.
+ */
+int mi_query_launch(int n, int pivot, int64_t batch, int threads_per_block, int* form, int* lanes_per_matrix,
+                    int* matrices_per_warp, int* threads_per_block_used);
 
 /*
  * Mixed sizes in one call.  Matrix i is n_i x n_i (1..32), row-major at

@@ -22,6 +22,7 @@ __all__ = [
     "batched_inverse",
     "batched_inverse_",
     "query_config",
+    "query_launch",
     "MatrixInversionError",
     "PIVOT_MODES",
     "pivot_mode",
@@ -121,7 +122,9 @@ def batched_inverse(A, pivot=True, *, return_perm: bool = True, return_info: boo
 
 
 def query_config(n: int) -> dict:
-    """Launch geometry for size n (lanes per matrix, matrices per warp, ...)."""
+    """Launch geometry for size n without pivoting or with the reference
+    rules on large batches (lanes per matrix, matrices per warp, ...);
+    :func:`query_launch` covers every pivot mode and batch size."""
     L = _lib.load()
     vals = [ctypes.c_int() for _ in range(4)]
     _lib.check(L.mi_query_config(int(n), *[ctypes.byref(v) for v in vals]))
@@ -130,4 +133,25 @@ def query_config(n: int) -> dict:
         "matrices_per_warp": vals[1].value,
         "smem_bytes_per_warp": vals[2].value,
         "default_threads_per_block": vals[3].value,
+    }
+
+
+def query_launch(n: int, pivot=True, batch: int = 1_000_000, threads_per_block: int = 0) -> dict:
+    """The kernel a contiguous ``batched_inverse_`` call of ``batch`` n x n
+    matrices launches: its form ("thread": one thread per matrix; "lanes": a
+    group of lanes per matrix; "rows": 16 lanes per matrix owning whole rows,
+    partial pivoting), lanes per matrix, matrices per warp and threads per
+    block.  ``knob`` says whether ``threads_per_block`` (the NUMTHREADS knob)
+    reaches the launch -- the lane-group form only.  Needs no GPU."""
+    L = _lib.load()
+    vals = [ctypes.c_int() for _ in range(4)]
+    _lib.check(L.mi_query_launch(int(n), pivot_mode(pivot), int(batch), int(threads_per_block),
+                                 *[ctypes.byref(v) for v in vals]))
+    form = vals[0].value
+    return {
+        "form": _lib.FORM_NAMES[form],
+        "lanes_per_matrix": vals[1].value,
+        "matrices_per_warp": vals[2].value,
+        "threads_per_block": vals[3].value,
+        "knob": form == _lib.MI_FORM_LANES,
     }

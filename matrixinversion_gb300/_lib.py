@@ -18,6 +18,10 @@ MI_ERR_CUDA = -4
 MI_ERR_SCRATCH_LIMIT = -5
 MI_NOALLOC_MAX_COUNT = 262144
 
+# kernel forms reported by mi_query_launch
+MI_FORM_THREAD, MI_FORM_LANES, MI_FORM_ROWS = 1, 2, 3
+FORM_NAMES = {MI_FORM_THREAD: "thread", MI_FORM_LANES: "lanes", MI_FORM_ROWS: "rows"}
+
 PIVOT_MODES = {"none": 0, "reference": 1, "reference_serial": 2, "partial": 3}
 
 _lib = None
@@ -51,6 +55,8 @@ def load(path: str | None = None):
     ip = ctypes.POINTER(ctypes.c_int)
     L.mi_query_config.argtypes = [i32, ip, ip, ip, ip]
     L.mi_query_config.restype = i32
+    L.mi_query_launch.argtypes = [i32, i32, i64, i32, ip, ip, ip, ip]
+    L.mi_query_launch.restype = i32
     L.mi_error_string.argtypes = [i32]
     L.mi_error_string.restype = ctypes.c_char_p
     L.mi_last_cuda_error.argtypes = []

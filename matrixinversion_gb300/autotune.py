@@ -2,11 +2,15 @@
 
 For each (n, pivot mode) it times the kernel at every candidate
 threads-per-block value (matrices per block = threads / lanes per matrix,
-lanes per matrix from mi_query_config) on a seeded uniform batch, each launch
+lanes per matrix from mi_query_launch) on a seeded uniform batch, each launch
 on a fresh copy of the batch, and installs the fastest with
 mi_set_launch_config.  Both entry points use the installed value whenever the
-caller passes threads_per_block = 0: the contiguous call and every bucket of
-a descriptor call.  Tables can be saved and loaded as JSON.
+caller passes threads_per_block = 0: the contiguous call and the lane-group
+buckets of a descriptor call.  Sizes whose contiguous launch at the tuning
+batch has a fixed block (one thread per matrix, or whole rows per lane in
+partial mode: mi_query_launch) are not timed -- the knob does not reach that
+launch -- and are reported with ``best`` 0 and their form.  Tables can be
+saved and loaded as JSON.
 
     python -m matrixinversion_gb300.autotune --n 2-32 --modes none,reference --out tuned.json
 """
@@ -44,15 +48,26 @@ def _time_one(n: int, mode: str, tpb: int, src, work, iters: int) -> float:
 
 def tune(ns=range(1, 33), modes=("none", "reference"), batch: int = 262144, iters: int = 5,
          candidates=CANDIDATES, install: bool = True, seed: int = 0) -> dict:
-    """{(n, mode): {"best": tpb, "ms": {tpb: ms}}}; installs the best values."""
+    """{(n, mode): {"best": tpb, "ms": {tpb: ms}}}; installs the best values.
+
+    Pairs the knob does not reach at `batch` get {"best": 0, "ms": {},
+    "form": <form>} and nothing is installed for them."""
     import torch
+
+    import matrixinversion_gb300 as mi
 
     table = {}
     g = torch.Generator(device="cuda").manual_seed(seed)
     for n in ns:
+        tunable = [m for m in modes if mi.query_launch(n, m, batch)["knob"]]
+        for m in modes:
+            if m not in tunable:
+                table[(n, m)] = {"best": 0, "ms": {}, "form": mi.query_launch(n, m, batch)["form"]}
+        if not tunable:
+            continue
         src = torch.rand(batch, n, n, generator=g, device="cuda") * 2 - 1
         work = torch.empty_like(src)
-        for mode in modes:
+        for mode in tunable:
             s = src + n * torch.eye(n, device="cuda") if mode == "none" else src
             ms = {tpb: _time_one(n, mode, tpb, s, work, iters) for tpb in candidates}
             best = min(ms, key=ms.get)
@@ -82,10 +97,12 @@ def save(table: dict, path: str) -> None:
 def load(path: str, install: bool = True) -> dict:
     with open(path) as f:
         rows = json.load(f)
-    table = {(r["n"], r["mode"]): {"best": r["best"], "ms": {int(k): t for k, t in r["ms"].items()}} for r in rows}
+    table = {(r["n"], r["mode"]): {"best": r["best"], "ms": {int(k): t for k, t in r["ms"].items()},
+                                   **({"form": r["form"]} if "form" in r else {})} for r in rows}
     if install:
         for (n, m), v in table.items():
-            set_config(n, m, v["best"])
+            if v["best"]:
+                set_config(n, m, v["best"])
     return table
 
 
@@ -101,6 +118,9 @@ def main(argv=None):
     a = p.parse_args(argv)
     table = tune(parse_range(a.n), a.modes.split(","), a.batch, a.iters)
     for (n, m), v in sorted(table.items()):
+        if not v["best"]:
+            print(json.dumps({"n": n, "mode": m, "fixed_block": v["form"]}), flush=True)
+            continue
         print(json.dumps({"n": n, "mode": m, "best": v["best"], "ms_best": round(v["ms"][v["best"]], 4),
                           "ms_default": round(v["ms"].get(128, float("nan")), 4)}), flush=True)
     if a.out:

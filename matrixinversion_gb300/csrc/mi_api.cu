@@ -20,7 +20,6 @@ static int cuda_fail(cudaError_t e, const char* what) {
 
 int set_cuda_error(cudaError_t e, const char* what) { return cuda_fail(e, what); }
 
-// Threads per block per (n, pivot mode): 0 = the default; set by the autotuner.
 // Threads per block per (n, pivot mode), measured on GB300 by the autotuner
 // (matrixinversion_gb300/autotune.py: 262,144 uniform matrices per size, the
 // fastest of 32..256; reference_serial uses the reference column); 0 = the
@@ -142,6 +141,39 @@ static bool query(int n, int& lanes, int& mpw, int& smem_warp) {
     }
 }
 
+static_assert(kFormThread == MI_FORM_THREAD && kFormLanes == MI_FORM_LANES && kFormRows == MI_FORM_ROWS,
+              "kernel form codes of the ABI");
+
+// The threads-per-block knob as a contiguous call resolves it: 0 = the
+// installed entry for (n, mode); rounded up to a multiple of 32, capped.
+static int resolve_threads(int n, int mode, int threads_per_block) {
+    int tpb = threads_per_block == 0 ? tuned_threads(n, mode) : threads_per_block;
+    tpb = (tpb + 31) / 32 * 32;
+    return tpb > kMaxThreadsPerBlock ? kMaxThreadsPerBlock : tpb;
+}
+
+template <int N>
+static LaunchForm form_for_mode(int mode, long long batch, int tpb) {
+    switch (mode) {
+        case kModeNone: return launch_form<N, kModeNone>(batch, tpb);
+        case kModeReference: return launch_form<N, kModeReference>(batch, tpb);
+        case kModeReferenceSerial: return launch_form<N, kModeReferenceSerial>(batch, tpb);
+        default: return launch_form<N, kModePartial>(batch, tpb);
+    }
+}
+
+static bool query_launch(int n, int mode, long long batch, int tpb, LaunchForm& out) {
+    switch (n) {
+#define MI_L(K) case K: out = form_for_mode<K>(mode, batch, tpb); return true;
+        MI_L(1) MI_L(2) MI_L(3) MI_L(4) MI_L(5) MI_L(6) MI_L(7) MI_L(8)
+        MI_L(9) MI_L(10) MI_L(11) MI_L(12) MI_L(13) MI_L(14) MI_L(15) MI_L(16)
+        MI_L(17) MI_L(18) MI_L(19) MI_L(20) MI_L(21) MI_L(22) MI_L(23) MI_L(24)
+        MI_L(25) MI_L(26) MI_L(27) MI_L(28) MI_L(29) MI_L(30) MI_L(31) MI_L(32)
+#undef MI_L
+        default: return false;
+    }
+}
+
 }  // namespace mi
 
 extern "C" {
@@ -187,12 +219,24 @@ int mi_inverse_cfg_f32(float* d_a, int32_t* d_perm, int32_t* d_info, int64_t bat
     if (batch == 0) return MI_OK;
     if (d_a == nullptr) return MI_ERR_NULL_POINTER;
     if ((reinterpret_cast<uintptr_t>(d_a) & 3u) != 0) return MI_ERR_MISALIGNED;
-    int tpb = threads_per_block == 0 ? mi::tuned_threads(n, pivot) : threads_per_block;
-    tpb = (tpb + 31) / 32 * 32;
-    if (tpb > mi::kMaxThreadsPerBlock) tpb = mi::kMaxThreadsPerBlock;
+    const int tpb = mi::resolve_threads(n, pivot, threads_per_block);
     cudaError_t e = table[n](d_a, d_perm, d_info, (long long)batch, tpb, grid_blocks,
                              reinterpret_cast<cudaStream_t>(stream));
     if (e != cudaSuccess) return mi::cuda_fail(e, "mi_inverse launch");
+    return MI_OK;
+}
+
+int mi_query_launch(int n, int pivot, int64_t batch, int threads_per_block, int* form, int* lanes_per_matrix,
+                    int* matrices_per_warp, int* threads_per_block_used) {
+    if (n < 1 || n > 32 || pivot < MI_PIVOT_NONE || pivot > MI_PIVOT_PARTIAL || batch < 0 || threads_per_block < 0)
+        return MI_ERR_INVALID_VALUE;
+    mi::LaunchForm f{};
+    if (!mi::query_launch(n, pivot, (long long)batch, mi::resolve_threads(n, pivot, threads_per_block), f))
+        return MI_ERR_INVALID_VALUE;
+    if (form) *form = f.form;
+    if (lanes_per_matrix) *lanes_per_matrix = f.lanes;
+    if (matrices_per_warp) *matrices_per_warp = f.mpw;
+    if (threads_per_block_used) *threads_per_block_used = f.threads;
     return MI_OK;
 }
 

@@ -102,6 +102,30 @@ cudaError_t launch(float* a, int32_t* perm, int32_t* info, long long batch, int 
     return cudaGetLastError();
 }
 
+// What launch<N, MODE> runs for a contiguous batch: the kernel form (the
+// MI_FORM_* codes of mi_inverse.h), lanes per matrix, matrices per warp and
+// threads per block.  The branches are launch<N, MODE>'s, in its order; only
+// the lane-group form launches with the resolved threads-per-block knob
+// `tpb`, the other two have a fixed block.
+enum : int { kFormThread = 1, kFormLanes = 2, kFormRows = 3 };
+
+struct LaunchForm {
+    int form, lanes, mpw, threads;
+};
+
+template <int N, int MODE>
+LaunchForm launch_form(long long batch, int tpb) {
+    if constexpr (N <= kTinyMax) {
+        return {kFormThread, 1, 32, tiny_threads<N>()};
+    } else if constexpr (N <= tiny_max_contig<MODE>()) {
+        if (batch >= tiny_min_batch<N, MODE>()) return {kFormThread, 1, 32, tiny_threads<N>()};
+    }
+    if constexpr (MODE == kModePartial && N >= kRowsMin && rows_partial_enabled<N>())
+        return {kFormRows, kRowsLanes, kRowsMats, 32 * kRowsWarps};
+    constexpr int L = default_lanes(N, MODE);
+    return {kFormLanes, L, Geom<N, L>::M, tpb};
+}
+
 // Indexed bucket launch: the kernel reads its bucket's [start, count) from
 // `range` on the device, so the grid is fixed (persistent warps) and the
 // launch needs no host round trip -- it can be captured in a CUDA graph.

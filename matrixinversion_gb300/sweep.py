@@ -105,6 +105,8 @@ def run_case(n: int, batch: int, pivot: str, runs: int, threads: int, with_cubla
         "hbm_roofline_frac": batch * bytes_per / (avg / 1e3) / 1e9 / hbm_peak_gbs(),
         "residual": residual_stats(src, X, sample),
         "singular": int((info != 0).sum().item()),
+        # the kernel form that ran; NUMTHREADS reaches only the lane-group form
+        "launch": mi.query_launch(n, pivot, batch, threads),
     }
     del X, w
     if with_cublas:

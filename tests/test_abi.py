@@ -86,3 +86,80 @@ def test_python_surface_rejects_host_tensors():
     assert mi.pivot_mode("partial") == 3 and mi.pivot_mode("reference_serial") == 2
     with pytest.raises(ValueError):
         mi.pivot_mode("lapack")
+
+
+def test_query_launch_reports_the_form_each_call_runs(lib):
+    """mi_query_launch follows the contiguous launch's choice of kernel form."""
+    import matrixinversion_gb300 as mi
+    from matrixinversion_gb300 import _lib
+
+    def q(n, pivot, batch, tpb=0):
+        r = mi.query_launch(n, pivot, batch, tpb)
+        return r["form"], r["lanes_per_matrix"], r["matrices_per_warp"], r["threads_per_block"], r["knob"]
+
+    # n <= 8: one thread per matrix at any batch, 4 warps per block
+    for pivot in ("none", "reference", "reference_serial", "partial"):
+        assert q(8, pivot, 10) == ("thread", 1, 32, 128, False)
+        assert q(1, pivot, 10**6, 256) == ("thread", 1, 32, 128, False)
+    # n = 9..15: one thread per matrix on large batches (2 warps per block up
+    # to n = 13, 1 above), lane groups below the measured crossover
+    assert q(12, "reference", 10**6) == ("thread", 1, 32, 64, False)
+    assert q(15, "none", 12288) == ("thread", 1, 32, 32, False)
+    assert q(12, "reference", 12287, 64) == ("lanes", 8, 4, 64, True)
+    assert q(12, "partial", 4096) == ("thread", 1, 32, 64, False)
+    assert q(12, "partial", 4095, 32) == ("lanes", 16, 2, 32, True)
+    # the knob as mi_inverse_cfg_f32 resolves it: 0 = installed entry,
+    # rounded up to a warp multiple, capped at 256
+    assert q(20, "reference", 1000, 65)[3] == 96
+    assert q(20, "reference", 1000, 300)[3] == 256
+    assert q(20, "reference", 1000, 0)[3] == lib_tuned(lib, 20, 1)
+    # partial pivoting: whole rows per lane at n = 16..28 and 32, one matrix
+    # per warp in lane blocks at n = 29..31
+    for n in (16, 17, 24, 28, 32):
+        assert q(n, "partial", 10**6, 64) == ("rows", 16, 2, 128, False), n
+    for n in (29, 30, 31):
+        assert q(n, "partial", 10**6, 64) == ("lanes", 32, 1, 64, True), n
+    assert q(32, "reference", 10**6, 128) == ("lanes", 16, 2, 128, True)
+    # argument errors
+    for bad in ((0, 1, 10, 0), (33, 1, 10, 0), (8, 4, 10, 0), (8, -1, 10, 0), (8, 1, -1, 0), (8, 1, 10, -32)):
+        assert lib.mi_query_launch(*bad, None, None, None, None) == _lib.MI_ERR_INVALID_VALUE, bad
+
+
+def lib_tuned(lib, n, pivot):
+    v = ctypes.c_int()
+    assert lib.mi_get_launch_config(n, pivot, ctypes.byref(v)) == 0
+    return v.value
+
+
+def test_noalloc_and_descriptor_argument_checks_without_gpu(lib):
+    """The descriptor entry points validate their arguments before any CUDA call."""
+    from matrixinversion_gb300 import _lib
+
+    d = lib.mi_inverse_descr_f32
+    assert d(None, None, None, None, None, None, 0, 0, 0, None, 0, None) == _lib.MI_OK
+    assert d(None, None, None, None, None, None, -1, 0, 0, None, 0, None) == _lib.MI_ERR_INVALID_VALUE
+    assert d(None, None, None, None, None, None, 4, 0, 0, None, 0, None) == _lib.MI_ERR_NULL_POINTER
+    p = ctypes.c_void_p(0x100000)
+    assert d(ctypes.c_void_p(0x100002), p, p, p, None, None, 4, 0, 0, p, 1 << 20, None) == _lib.MI_ERR_MISALIGNED
+    assert d(p, p, p, p, None, None, 4, 0, 0, ctypes.c_void_p(0x100010), 1 << 20, None) == _lib.MI_ERR_MISALIGNED
+    need = lib.mi_descr_workspace_bytes(4)
+    assert d(p, p, p, p, None, None, 4, 0, 0, p, need - 1, None) == _lib.MI_ERR_INVALID_VALUE
+    for count in (0, 1, 1000, 262144):
+        assert lib.mi_descr_workspace_bytes(count) == (4096 + 4 * count + 255) // 256 * 256
+    na = lib.mi_inverse_descr_noalloc_f32
+    assert na(None, None, None, None, None, None, 0, 0, 0, None) == _lib.MI_OK
+    assert na(None, None, None, None, None, None, -5, 0, 0, None) == _lib.MI_ERR_INVALID_VALUE
+    assert na(p, p, p, p, None, None, _lib.MI_NOALLOC_MAX_COUNT + 1, 0, 0, None) == _lib.MI_ERR_SCRATCH_LIMIT
+    # refinement entry points
+    assert lib.mi_newton_schulz_f32(None, None, 4, 16, 1, None) == _lib.MI_ERR_INVALID_VALUE
+    assert lib.mi_newton_schulz_f32(None, None, 4, 32, 5, None) == _lib.MI_ERR_INVALID_VALUE
+    assert lib.mi_newton_schulz_f32(None, None, 0, 32, 1, None) == _lib.MI_OK
+    assert lib.mi_newton_schulz_f32(None, None, 4, 32, 1, None) == _lib.MI_ERR_NULL_POINTER
+    assert lib.mi_newton_schulz_f32(ctypes.c_void_p(0x100004), p, 4, 32, 1, None) == _lib.MI_ERR_MISALIGNED
+    for f in (lib.mi_refine_fp64_f32, lib.mi_refine_df_f32):
+        assert f(None, None, None, 4, 4, 33, None) == _lib.MI_ERR_INVALID_VALUE
+        assert f(None, None, None, 0, 4, 32, None) == _lib.MI_OK
+        assert f(None, None, None, 4, 4, 32, None) == _lib.MI_ERR_NULL_POINTER
+    assert lib.mi_refine_df_next_f32(p, p, p, 4, 4, 32, -1.0, p, None) == _lib.MI_ERR_INVALID_VALUE
+    assert lib.mi_flag_condition_f32(None, None, 4, 0, 8.0, None, None) == _lib.MI_ERR_INVALID_VALUE
+    assert lib.mi_flag_condition_f32(None, None, 4, 32, 8.0, None, None) == _lib.MI_ERR_NULL_POINTER

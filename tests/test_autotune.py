@@ -33,15 +33,32 @@ def test_set_get_and_file_round_trip(lib, tmp_path):
             autotune.set_config(*bad)
 
 
+def test_skipped_pairs_round_trip_and_install_nothing(lib, tmp_path):
+    shipped = autotune.get_config(8, "none")
+    table = {(8, "none"): {"best": 0, "ms": {}, "form": "thread"},
+             (20, "reference"): {"best": 64, "ms": {64: 1.0, 256: 1.5}}}
+    path = str(tmp_path / "t.json")
+    autotune.save(table, path)
+    assert autotune.load(path) == table
+    assert autotune.get_config(8, "none") == shipped              # a fixed-block pair installs nothing
+    assert autotune.get_config(20, "reference") == 64
+    autotune.set_config(20, "reference", 0)
+
+
 @pytest.mark.gpu
 def test_tuning_installs_best_and_keeps_results(mi_gpu, oracle):
     import torch
 
-    A = torch.from_numpy(oracle.uniform(4, 3000, 8)).cuda()
+    # n = 20 with the reference rule runs the lane-group form, whose block
+    # size is the knob; n = 8 runs one thread per matrix with a fixed block
+    A = torch.from_numpy(oracle.uniform(4, 3000, 20)).cuda()
     ref, _, _ = mi_gpu.batched_inverse(A, "reference")
-    table = autotune.tune([8], ["reference"], batch=4096, iters=2, candidates=(64, 256))
-    best = table[(8, "reference")]["best"]
-    assert best in (64, 256) and autotune.get_config(8, "reference") == best
+    shipped8 = autotune.get_config(8, "reference")
+    table = autotune.tune([8, 20], ["reference"], batch=4096, iters=2, candidates=(64, 256))
+    assert table[(8, "reference")] == {"best": 0, "ms": {}, "form": "thread"}
+    assert autotune.get_config(8, "reference") == shipped8
+    best = table[(20, "reference")]["best"]
+    assert best in (64, 256) and autotune.get_config(20, "reference") == best
     X, _, _ = mi_gpu.batched_inverse(A, "reference")
     assert torch.equal(X, ref)
-    autotune.set_config(8, "reference", 0)
+    autotune.set_config(20, "reference", 0)
