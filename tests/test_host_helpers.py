@@ -1,0 +1,89 @@
+"""Host-side helpers of the workloads and the descriptor batch.  CPU only.
+
+Descriptor packing and masks, the sweep's range syntax (MATRIXSIZE /
+NUMMATRICES values such as "2-32" or "1000,1000000"), the seeded input
+generators against the oracle's MT19937 stream, and the precision workload's
+condition numbers.
+"""
+import numpy as np
+import pytest
+
+
+def test_pack_unpack_round_trip_and_alignment():
+    from matrixinversion_gb300 import descr, data
+
+    rng = np.random.RandomState(3)
+    ns = [int(n) for n in rng.randint(1, 33, size=200)]
+    mats = [data.uniform(100 + i, 1, n)[0] for i, n in enumerate(ns)]
+    for align in (1, 4, 8):
+        packed, offsets, got_ns = descr.pack(mats, align=align)
+        assert packed.dtype == np.float32 and offsets.dtype == np.int64 and got_ns.dtype == np.int32
+        assert list(got_ns) == ns
+        assert np.all(offsets % align == 0)
+        ends = offsets + got_ns.astype(np.int64) ** 2
+        assert np.all(offsets[1:] >= ends[:-1])                 # no overlap, in order
+        assert ends[-1] <= packed.size
+        for a, b in zip(mats, descr.unpack(packed, offsets, got_ns)):
+            assert np.array_equal(a, b)
+        if align == 1:
+            assert packed.size == sum(n * n for n in ns)          # densely packed
+    packed, offsets, got_ns = descr.pack([])
+    assert packed.size == 1 and offsets.size == 0 and got_ns.size == 0
+
+
+def test_masks_cover_exactly_the_sizes_and_modes_present():
+    from matrixinversion_gb300 import descr
+
+    n_mask, mode_mask = descr.masks([1, 5, 5, 32], [0, 3, 3, 0])
+    assert n_mask == (1 << 0) | (1 << 4) | (1 << 31)
+    assert mode_mask == 0b1001
+    # malformed entries (the kernel reports them through info = -1) add no bits
+    assert descr.masks([0, 33, 7], [4, -1, 2]) == (1 << 6, 1 << 2)
+
+
+def test_parse_range():
+    from matrixinversion_gb300.sweep import parse_range
+
+    assert parse_range("2-5") == [2, 3, 4, 5]
+    assert parse_range("32") == [32]
+    assert parse_range("2-4,8,16-17") == [2, 3, 4, 8, 16, 17]
+    assert parse_range("1000,1000000") == [1000, 1000000]
+
+
+@pytest.mark.parametrize("n", [1, 7, 32])
+def test_generators_match_the_oracle_stream(oracle, n):
+    from matrixinversion_gb300 import data
+
+    A = data.uniform(11, 50, n)
+    assert A.dtype == np.float32 and A.shape == (50, n, n)
+    assert np.array_equal(A, oracle.uniform(11, 50, n))
+    assert A.min() >= -1.0 and A.max() < 1.0
+    # 2^-23 grid of [-1, 1): every value is an integer multiple of 2^-23
+    assert np.array_equal(np.round(A * 2.0**23), A * 2.0**23)
+    D = data.diagonally_dominant(11, 50, n)
+    assert np.array_equal(D, A + np.float32(n) * np.eye(n, dtype=np.float32))    # FP32 sum, as generated
+    D32 = data.diagonally_dominant(0, 3, n, shift=32.0)
+    assert np.array_equal(D32, data.uniform(0, 3, n) + np.float32(32.0) * np.eye(n, dtype=np.float32))
+    off = ~np.eye(n, dtype=bool)
+    assert np.array_equal(D32[:, off], data.uniform(0, 3, n)[:, off])
+
+
+@pytest.mark.parametrize("kappa", [1e1, 1e3, 1e5])
+def test_conditioned_matrices_hit_their_bucket(kappa):
+    from matrixinversion_gb300 import refine
+
+    A = refine.conditioned(8, kappa, n=32, seed=5, device="cpu").double().numpy()
+    c = np.linalg.cond(A)
+    # the FP32 rounding of A moves the smallest singular value by ~kappa * 2^-24
+    assert np.all(np.abs(c / kappa - 1.0) < 0.01 + kappa * 2.0**-24 * 8), c
+
+
+def test_rel_error_is_max_abs_over_max_abs():
+    import torch
+
+    from matrixinversion_gb300 import refine
+
+    X64 = torch.tensor([[[2.0, -4.0], [1.0, 0.5]]], dtype=torch.float64)
+    X = (X64 + torch.tensor([[[0.0, 0.0], [0.1, 0.0]]], dtype=torch.float64)).float()
+    r = refine.rel_error(X, X64)
+    assert r.shape == (1,) and abs(float(r[0]) - 0.1 / 4.0) < 1e-7
