@@ -62,6 +62,23 @@ namespace mi {
 enum : int { kModeNone = 0, kModeReference = 1, kModeReferenceSerial = 2, kModePartial = 3 };
 enum : int { kCopyPlain = 0, kCopyBulk = 1, kCopyTensor = 2, kCopyWindow = 3 };
 
+// Dynamic shared memory above the 48 KB default needs an opt-in per kernel,
+// and the opt-in holds for one device only.  `done` has one zero-initialised
+// entry per device and records the largest size opted in there; sizes only
+// grow, so a launch never finds its kernel's limit lowered by another.
+constexpr int kMaxDevices = 64;
+
+template <typename Kernel>
+inline cudaError_t opt_in_smem(Kernel kern, size_t smem, size_t* done) {
+    if (smem <= 48 * 1024) return cudaSuccess;
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) dev = -1;
+    if (dev >= 0 && done[dev] >= smem) return cudaSuccess;
+    const cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess && dev >= 0) done[dev] = smem;
+    return e;
+}
+
 constexpr unsigned kFull = 0xffffffffu;
 // Longest wait for one tile copy (SM clocks, about 2 s) before the kernel
 // gives up, records an error and returns.

@@ -59,11 +59,10 @@ cudaError_t launch(float* a, int32_t* perm, int32_t* info, long long batch, int 
     const int warps = tpb / 32;
     const size_t smem = smem_bytes<N, L, MODE>(warps);
     auto kern = mi_inverse_kernel<N, L, MODE>;
-    static size_t smem_set = 0;                     // largest dynamic size opted in so far
-    if (smem > 48 * 1024 && smem > smem_set) {
-        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    static size_t smem_set[kMaxDevices] = {};       // largest dynamic size opted in, per device
+    {
+        const cudaError_t e = opt_in_smem(kern, smem, smem_set);
         if (e != cudaSuccess) return e;
-        smem_set = smem;
     }
 
     // how each warp's group of M matrices moves in: tensor copies (rows of a
@@ -141,11 +140,10 @@ cudaError_t launch_indexed(float* base, const long long* offsets, const int* lis
     const int warps = tpb / 32;
     const size_t smem = smem_bytes<N, L, MODE>(warps);
     auto kern = mi_inverse_indexed_kernel<N, L, MODE>;
-    static size_t smem_set = 0;
-    if (smem > 48 * 1024 && smem > smem_set) {
-        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    static size_t smem_set[kMaxDevices] = {};
+    {
+        const cudaError_t e = opt_in_smem(kern, smem, smem_set);
         if (e != cudaSuccess) return e;
-        smem_set = smem;
     }
     if (grid <= 0) {
         static int per_sm_cached[9] = {0};

@@ -231,11 +231,10 @@ extern "C" int mi_newton_schulz_f32(const float* d_a, float* d_x, int64_t batch,
     if ((reinterpret_cast<uintptr_t>(d_a) & 15u) != 0 || (reinterpret_cast<uintptr_t>(d_x) & 15u) != 0)
         return MI_ERR_MISALIGNED;
     const size_t smem = sizeof(mi::ns::Smem) + 128;
-    static bool attr = false;
-    if (!attr) {
-        cudaError_t e = cudaFuncSetAttribute(mi::mi_ns_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    static size_t smem_set[mi::kMaxDevices] = {};
+    {
+        const cudaError_t e = mi::opt_in_smem(mi::mi_ns_kernel, smem, smem_set);
         if (e != cudaSuccess) return mi::set_cuda_error(e, "newton-schulz attributes");
-        attr = true;
     }
     const long long tiles = (batch + 3) / 4;
     long long grid = 2LL * mi::device_sm_count();

@@ -292,12 +292,13 @@ cudaError_t launch_rows_partial(float* a, int32_t* perm, int32_t* info, long lon
     constexpr int threads = 32 * kRowsWarps;
     constexpr size_t smem = (size_t)kRowsWarps * G::kWarp * sizeof(float);
     auto kern = mi_rows_partial_kernel<N>;
+    static size_t smem_set[kMaxDevices] = {};
+    {
+        const cudaError_t e = opt_in_smem(kern, smem, smem_set);
+        if (e != cudaSuccess) return e;
+    }
     static int per_sm = 0;
     if (per_sm == 0) {
-        if (smem > 48 * 1024) {
-            cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            if (e != cudaSuccess) return e;
-        }
         cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem);
         if (e != cudaSuccess) return e;
         if (per_sm < 1) per_sm = 1;
