@@ -22,6 +22,9 @@ LIBDIR = os.path.join(PKG, "lib")
 LIB = os.path.join(LIBDIR, "libmi_inverse.so")
 CSRC_CMP = os.path.join(PKG, "csrc_compare")
 LIB_CUBLAS = os.path.join(LIBDIR, "libmi_cublas_ref.so")
+DRIVER_SRC = os.path.join(PKG, "driver", "mi_driver.cpp")
+BINDIR = os.path.join(PKG, "bin")
+DRIVER = os.path.join(BINDIR, "mi_driver")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I" + INCLUDE, "-I" + CSRC]
@@ -83,5 +86,27 @@ def build_comparator() -> str:
     return LIB_CUBLAS
 
 
+
+def build_driver() -> str:
+    """The command-line driver ``bin/mi_driver`` (the reference's per-run
+    stdout contract over the C ABI), linked against ``lib/libmi_inverse.so``
+    through an rpath relative to the binary.  Built on demand, not by
+    :func:`build`: the library does not depend on it."""
+    if not os.path.exists(LIB):
+        build()
+    os.makedirs(BINDIR, exist_ok=True)
+    newest = max(os.path.getmtime(DRIVER_SRC), os.path.getmtime(LIB), _deps())
+    if os.path.exists(DRIVER) and os.path.getmtime(DRIVER) >= newest:
+        return DRIVER
+    cmd = [nvcc(), "-O2", "-std=c++17", "-Xcompiler", "-pthread", "-I" + INCLUDE, DRIVER_SRC, "-o", DRIVER,
+           "-L" + LIBDIR, "-lmi_inverse", "-Xlinker", "-rpath", "-Xlinker", "$ORIGIN/../lib"]
+    out = subprocess.run(cmd, capture_output=True, text=True)
+    if out.returncode != 0:
+        raise RuntimeError("driver build failed:\n" + out.stderr[-4000:])
+    return DRIVER
+
+
 if __name__ == "__main__":
     print(build(verbose="-v" in sys.argv))
+    if "--driver" in sys.argv:
+        print(build_driver())
