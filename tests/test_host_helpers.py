@@ -87,3 +87,46 @@ def test_rel_error_is_max_abs_over_max_abs():
     X = (X64 + torch.tensor([[[0.0, 0.0], [0.1, 0.0]]], dtype=torch.float64)).float()
     r = refine.rel_error(X, X64)
     assert r.shape == (1,) and abs(float(r[0]) - 0.1 / 4.0) < 1e-7
+
+
+def test_clock_summary_reads_nvidia_smi_rows(tmp_path):
+    """The bench's clock record: median SM clock over the loaded samples and
+    every throttle reason seen Active (the rows nvidia-smi prints with
+    --format=csv,noheader,nounits)."""
+    import bench
+
+    rows = ["0, 345, 2070, 110.5, 0x0000000000000000, Not Active, Not Active, Not Active, Not Active"] * 3
+    rows += [f"0, {mhz}, 2070, 1200.0, 0x0000000000000000, Not Active, Not Active, Not Active, Not Active"
+             for mhz in (1965, 1980, 2010)]
+    rows += ["0, 1500, 2070, 1390.0, 0x0000000000000004, Not Active, Not Active, Not Active, Active",
+             "0, [N/A], [N/A], [N/A], [N/A], [N/A], [N/A], [N/A], [N/A]"]
+    cs = bench.ClockSampler(0)
+    cs.file = open(tmp_path / "clocks.csv", "w+")
+    cs.file.write("\n".join(rows) + "\n")
+    s = cs.summary()
+    assert s["sm_max_mhz"] == 2070.0 and s["samples"] == len(rows)
+    assert s["sm_mhz"] == 1980.0                       # idle samples below half the peak are left out
+    assert s["reasons"] == ["sw_power_cap"]
+
+
+def test_reference_arm_line(capsys):
+    """bench.py --impl reference: the oracle's port of the reference algorithm
+    on the host cores, one JSON line with the contract's keys."""
+    import argparse
+    import json
+
+    import bench
+
+    args = argparse.Namespace(gpus=1, steps=1, warmup=0, impl="reference", n=8, batch=1000, pivot="reference",
+                              seed=0, no_e2e=True, no_cpu=False)
+    bench.run_reference_arm(args, rank=0)
+    line = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["unit"] == "matrices/s" and line["value"] > 0
+    assert line["metric"] == bench.METRIC and line["higher_is_better"] is True
+    assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] >= 1
+    assert line["e2e"] == {"value": line["value"], "unit": "matrices/s", "h2d_bytes_per_step": 0,
+                           "d2h_bytes_per_step": 0}
+    assert line["config"]["n"] == 8 and line["config"]["pivot"] == "reference"
+    bench.run_reference_arm(args, rank=1)              # other ranks print nothing
+    assert capsys.readouterr().out == ""
+    assert bench.algorithmic_bytes(32) == 8324
