@@ -168,6 +168,24 @@ int mi_inverse_descr_noalloc_f32(float* d_packed, const int64_t* d_offsets, cons
                                  uint32_t n_mask, uint32_t mode_mask, void* stream);
 
 /*
+ * Waits that ran out on the device (no counterpart in the reference, whose
+ * kernels wait without a limit).  Every wait of the kernels on a tile copy or
+ * a tensor-core product gives up after about two seconds; the warp (or CTA)
+ * then records a flag and stops, leaving the rest of its matrices unwritten.
+ * The call still returned MI_OK, so a caller that must know checks here:
+ *   *flags  (nullable) the flags recorded since the last clear:
+ *           MI_DEVERR_COPY_TIMEOUT  a tile copy did not arrive (inverse kernels)
+ *           MI_DEVERR_MMA_TIMEOUT   a tensor-core product did not complete
+ *                                   (mi_newton_schulz_f32)
+ *   clear   != 0 resets the flags after reading them.
+ * Per device (the current one).  Synchronous: it reads after the work already
+ * issued to the legacy default stream; synchronise other streams first.
+ */
+#define MI_DEVERR_COPY_TIMEOUT 1
+#define MI_DEVERR_MMA_TIMEOUT 2
+int mi_device_error(int* flags, int clear);
+
+/*
  * Newton-Schulz refinement of n = 32 inverses on the tensor cores (no
  * reference counterpart: the reference computes in FP32 only, with its FP64
  * switch commented out, verify.hpp:9):  X <- X + X (I - A X), `steps` times

@@ -23,6 +23,7 @@ __all__ = [
     "batched_inverse_",
     "query_config",
     "query_launch",
+    "device_error",
     "MatrixInversionError",
     "PIVOT_MODES",
     "pivot_mode",
@@ -155,3 +156,15 @@ def query_launch(n: int, pivot=True, batch: int = 1_000_000, threads_per_block: 
         "threads_per_block": vals[3].value,
         "knob": form == _lib.MI_FORM_LANES,
     }
+
+
+def device_error(clear: bool = True) -> int:
+    """Flags of waits that ran out on the current device since the last clear
+    (0 = none; MI_DEVERR_COPY_TIMEOUT = 1: a tile copy never arrived,
+    MI_DEVERR_MMA_TIMEOUT = 2: a tensor-core product never completed).  The
+    affected calls returned normally with some matrices left unwritten.
+    Synchronise the streams that ran the work first."""
+    L = _lib.load()
+    v = ctypes.c_int(0)
+    _lib.check(L.mi_device_error(ctypes.byref(v), 1 if clear else 0))
+    return v.value

@@ -18,6 +18,9 @@ MI_ERR_CUDA = -4
 MI_ERR_SCRATCH_LIMIT = -5
 MI_NOALLOC_MAX_COUNT = 262144
 
+# flags of mi_device_error
+MI_DEVERR_COPY_TIMEOUT, MI_DEVERR_MMA_TIMEOUT = 1, 2
+
 # kernel forms reported by mi_query_launch
 MI_FORM_THREAD, MI_FORM_LANES, MI_FORM_ROWS = 1, 2, 3
 FORM_NAMES = {MI_FORM_THREAD: "thread", MI_FORM_LANES: "lanes", MI_FORM_ROWS: "rows"}
@@ -57,6 +60,8 @@ def load(path: str | None = None):
     L.mi_query_config.restype = i32
     L.mi_query_launch.argtypes = [i32, i32, i64, i32, ip, ip, ip, ip]
     L.mi_query_launch.restype = i32
+    L.mi_device_error.argtypes = [ip, i32]
+    L.mi_device_error.restype = i32
     L.mi_error_string.argtypes = [i32]
     L.mi_error_string.restype = ctypes.c_char_p
     L.mi_last_cuda_error.argtypes = []

@@ -5,6 +5,7 @@
 #include <cstdio>
 #include <cstring>
 #include <mutex>
+#include <vector>
 
 #include "mi_inverse.h"
 #include "mi_launch.cuh"
@@ -19,6 +20,23 @@ static int cuda_fail(cudaError_t e, const char* what) {
 }
 
 int set_cuda_error(cudaError_t e, const char* what) { return cuda_fail(e, what); }
+
+// Readers of the per-module device error words, registered while the library
+// loads (function-local statics: safe whatever the order of static
+// initialisation across translation units).
+static std::mutex& error_readers_mu() {
+    static std::mutex m;
+    return m;
+}
+static std::vector<device_error_reader>& error_readers() {
+    static std::vector<device_error_reader> v;
+    return v;
+}
+bool register_device_error_reader(device_error_reader fn) {
+    std::lock_guard<std::mutex> lock(error_readers_mu());
+    error_readers().push_back(fn);
+    return true;
+}
 
 // Threads per block per (n, pivot mode), measured on GB300 by the autotuner
 // (matrixinversion_gb300/autotune.py: 262,144 uniform matrices per size, the
@@ -223,6 +241,17 @@ int mi_inverse_cfg_f32(float* d_a, int32_t* d_perm, int32_t* d_info, int64_t bat
     cudaError_t e = table[n](d_a, d_perm, d_info, (long long)batch, tpb, grid_blocks,
                              reinterpret_cast<cudaStream_t>(stream));
     if (e != cudaSuccess) return mi::cuda_fail(e, "mi_inverse launch");
+    return MI_OK;
+}
+
+int mi_device_error(int* flags, int clear) {
+    int all = 0;
+    std::lock_guard<std::mutex> lock(mi::error_readers_mu());
+    for (mi::device_error_reader read : mi::error_readers()) {
+        const cudaError_t e = read(&all, clear != 0);
+        if (e != cudaSuccess) return mi::cuda_fail(e, "device error word");
+    }
+    if (flags) *flags = all;
     return MI_OK;
 }
 

@@ -84,8 +84,31 @@ constexpr unsigned kFull = 0xffffffffu;
 // gives up, records an error and returns.
 constexpr long long kWaitLimit = 4000000000LL;
 
-// Sticky device error word: bit 0 = a tile-copy wait timed out.
+// Sticky device error word: bit 0 = a tile-copy wait timed out, bit 1 = a
+// tensor-core wait timed out (the MI_DEVERR_* flags of mi_inverse.h).  Every
+// translation unit that includes this header is a module of its own with its
+// own copy, so each registers a host reader of its copy when the library
+// loads; mi_device_error() reads them all.
 __device__ int g_device_error;
+
+using device_error_reader = cudaError_t (*)(int* flags, bool clear);
+bool register_device_error_reader(device_error_reader fn);   // mi_api.cu
+
+namespace {
+cudaError_t read_device_error(int* flags, bool clear) {
+    int v = 0;
+    cudaError_t e = cudaMemcpyFromSymbol(&v, g_device_error, sizeof(int));
+    if (e != cudaSuccess) return e;
+    if (clear && v != 0) {
+        const int zero = 0;
+        e = cudaMemcpyToSymbol(g_device_error, &zero, sizeof(int));
+        if (e != cudaSuccess) return e;
+    }
+    *flags |= v;
+    return cudaSuccess;
+}
+[[maybe_unused]] const bool g_device_error_registered = register_device_error_reader(&read_device_error);
+}  // namespace
 
 __host__ __device__ constexpr int pow2_at_least(int n) { return n <= 4 ? 4 : (n <= 8 ? 8 : (n <= 16 ? 16 : 32)); }
 

@@ -163,3 +163,18 @@ def test_noalloc_and_descriptor_argument_checks_without_gpu(lib):
     assert lib.mi_refine_df_next_f32(p, p, p, 4, 4, 32, -1.0, p, None) == _lib.MI_ERR_INVALID_VALUE
     assert lib.mi_flag_condition_f32(None, None, 4, 0, 8.0, None, None) == _lib.MI_ERR_INVALID_VALUE
     assert lib.mi_flag_condition_f32(None, None, 4, 32, 8.0, None, None) == _lib.MI_ERR_NULL_POINTER
+
+
+def test_device_error_query_reports_cuda_failure_without_gpu(lib):
+    """mi_device_error reads every module's error word through CUDA; with no
+    device the first read fails and the call says so (status, message)."""
+    import torch
+
+    from matrixinversion_gb300 import _lib
+
+    if torch.cuda.is_available():
+        pytest.skip("checks the path without a device")
+    v = ctypes.c_int(-7)
+    assert lib.mi_device_error(ctypes.byref(v), 1) == _lib.MI_ERR_CUDA
+    assert v.value == -7                                   # untouched on failure
+    assert b"device error word" in lib.mi_last_cuda_error()
