@@ -1208,6 +1208,7 @@ __global__ void __launch_bounds__(256, 2) mi_inverse_kernel(float* __restrict__ 
     long long g = (long long)blockIdx.x * W + warp;
     uint32_t phase = 0;
     unsigned round = 0;
+    bool timed_out = false;
     if (g < groups) issue(g);
     while (g < groups) {
         const long long first = g * M;
@@ -1215,8 +1216,9 @@ __global__ void __launch_bounds__(256, 2) mi_inverse_kernel(float* __restrict__ 
         // a window copy lands at the group's offset within its 16-byte granule
         const int shift = (copy_mode == kCopyWindow && async_g) ? (int)((first * NN) & 3) : 0;
         if (async_g) {
-            if (!mbar_wait(sm.bar, phase & 1u, kWaitLimit)) {
-                atomicOr(&g_device_error, 1);
+            // lanes time their waits separately, so the warp decides together
+            if (!__all_sync(kFull, mbar_wait(sm.bar, phase & 1u, kWaitLimit))) {
+                timed_out = true;
                 break;
             }
             phase++;
@@ -1252,6 +1254,12 @@ __global__ void __launch_bounds__(256, 2) mi_inverse_kernel(float* __restrict__ 
         const long long mb = first + mslot;
         phase_perm_info<N, L, MODE>(sm.scr0, lane, mb < batch ? mb : -1, perm_out, N, info_out);
         g = gn;
+    }
+    if (timed_out) {
+        atomicOr(&g_device_error, 1);
+        // the copy may still land in this warp's slot: wait for it once more,
+        // bounded, before the warp leaves
+        mbar_wait(sm.bar, phase & 1u, kWaitLimit);
     }
     if (lane == 0) bulk_wait_all();
 }
@@ -1328,12 +1336,14 @@ __global__ void __launch_bounds__(256, 2) mi_inverse_indexed_kernel(float* __res
     long long g = (long long)blockIdx.x * W + warp;
     uint32_t phase = 0;
     unsigned round = 0;
+    bool timed_out = false;
     bool used_bar = false;
     if (g < groups) used_bar = issue(g);
     while (g < groups) {
         if (used_bar) {
-            if (!mbar_wait(sm.bar, phase & 1u, kWaitLimit)) {
-                atomicOr(&g_device_error, 1);
+            // lanes time their waits separately, so the warp decides together
+            if (!__all_sync(kFull, mbar_wait(sm.bar, phase & 1u, kWaitLimit))) {
+                timed_out = true;
                 break;
             }
             phase++;
@@ -1374,6 +1384,12 @@ __global__ void __launch_bounds__(256, 2) mi_inverse_indexed_kernel(float* __res
         }
         phase_perm_info<N, L, MODE>(sm.scr0, lane, idx[mslot], perm_out, 32, info_out);
         g = gn;
+    }
+    if (timed_out) {
+        atomicOr(&g_device_error, 1);
+        // the copy may still land in this warp's slot: wait for it once more,
+        // bounded, before the warp leaves
+        mbar_wait(sm.bar, phase & 1u, kWaitLimit);
     }
     if (lane == 0) bulk_wait_all();
 }

@@ -140,6 +140,9 @@ __global__ void __launch_bounds__(128, 2) mi_ns_kernel(const float* __restrict__
                 ns::mma3(tmem, sm.ah, sm.al, sm.bh, sm.bl);
                 tc_commit(&sm.bar);
                 ok = mbar_wait(&sm.bar, phase & 1u, kWaitLimit);
+                // a product still running when the CTA gives up writes TMEM that
+                // is freed on the way out: wait for it once more, bounded
+                if (!ok) mbar_wait(&sm.bar, phase & 1u, kWaitLimit);
             }
             // one thread waits; the whole CTA learns the outcome at the barrier
             if (__syncthreads_or(!ok)) { failed = true; break; }
@@ -160,6 +163,9 @@ __global__ void __launch_bounds__(128, 2) mi_ns_kernel(const float* __restrict__
                 ns::mma3(tmem, sm.xah, sm.xal, sm.bh, sm.bl);
                 tc_commit(&sm.bar);
                 ok = mbar_wait(&sm.bar, phase & 1u, kWaitLimit);
+                // a product still running when the CTA gives up writes TMEM that
+                // is freed on the way out: wait for it once more, bounded
+                if (!ok) mbar_wait(&sm.bar, phase & 1u, kWaitLimit);
             }
             if (__syncthreads_or(!ok)) { failed = true; break; }
             phase++;
