@@ -42,6 +42,19 @@ SIZES = (4, 8, 12, 16, 20, 24, 28, 32)
 PIVOT_PARTIAL = 3
 
 
+def nvtx_ranges():
+    """(push, pop) of NVTX host ranges, so a timeline profiler shows each
+    batch's admission and issue; no-ops where torch was built without NVTX."""
+    try:
+        import torch.cuda.nvtx as nv
+
+        nv.range_push("mi_serving")
+        nv.range_pop()
+        return nv.range_push, nv.range_pop
+    except Exception:
+        return (lambda msg: None), (lambda: None)
+
+
 @dataclass
 class Trace:
     """Requests in arrival order: arrival time (s), matrices k, size n, and
@@ -245,6 +258,7 @@ class CudaServer:
         free = [0, 1]
         i = 0
         completed = 0
+        push, pop = nvtx_ranges()
         if self.resident:
             self.ring_dev.copy_(self.pristine)
         self.torch.cuda.synchronize(self.dev)
@@ -259,7 +273,9 @@ class CudaServer:
             if free and i < nreq and t.arrival[i] <= now:
                 j = batcher.next_batch(i, now)
                 h = free.pop(0)
+                push(f"batch requests {i}-{j - 1}")
                 inflight.append((i, j, h, self._launch_batch(i, j, h, coalesce)))
+                pop()
                 i = j
         lat = done - t.arrival
         wall = float(np.nanmax(done))

@@ -78,3 +78,9 @@ def test_resident_mode_equals_host_mode(mi_gpu):
         for r in range(40):
             assert np.array_equal(res.results(r), host.results(r)), r
     assert res.offline(iters=2) > 0
+
+
+def test_nvtx_ranges_are_callable_without_a_profiler():
+    push, pop = serving.nvtx_ranges()
+    push("batch requests 0-3")
+    pop()
