@@ -47,6 +47,41 @@ def test_header_compiles_as_c(tmp_path):
                     str(src), "-o", str(tmp_path / "t.o")], check=True)
 
 
+C_CALLER = r"""
+#include <stdio.h>
+#include "mi_inverse.h"
+
+int main(void) {
+    int form, lanes, mpw, tpb;
+    if (mi_abi_version() != MI_ABI_VERSION) return 2;
+    if (mi_query_launch(32, MI_PIVOT_PARTIAL, 1000000, 0, &form, &lanes, &mpw, &tpb) != MI_OK) return 3;
+    printf("%d %d %d %d\n", form, lanes, mpw, tpb);
+    /* argument errors come back as status codes, before any CUDA call */
+    if (mi_inverse_f32(NULL, NULL, NULL, 4, 8, MI_PIVOT_REFERENCE, NULL) != MI_ERR_NULL_POINTER) return 4;
+    if (mi_inverse_f32(NULL, NULL, NULL, 4, 33, MI_PIVOT_REFERENCE, NULL) != MI_ERR_INVALID_VALUE) return 5;
+    printf("%s\n", mi_error_string(MI_ERR_NULL_POINTER));
+    return 0;
+}
+"""
+
+
+def test_c_caller_links_and_runs_without_gpu(lib, tmp_path):
+    """A plain C program includes the header, links libmi_inverse and runs the
+    calls that need no device."""
+    from matrixinversion_gb300 import build
+
+    src = tmp_path / "caller.c"
+    src.write_text(C_CALLER)
+    exe = tmp_path / "caller"
+    subprocess.run(["gcc", "-std=c99", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"), str(src), "-o",
+                    str(exe), "-L", build.LIBDIR, "-lmi_inverse", "-Wl,-rpath," + build.LIBDIR], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
+    assert out.returncode == 0, (out.returncode, out.stderr)
+    first, second = out.stdout.splitlines()[:2]
+    assert first == "3 16 2 128"            # whole rows per lane, 16 lanes, 2 matrices per warp, 4 warps
+    assert "null" in second
+
+
 def test_query_and_errors_without_gpu(lib):
     from matrixinversion_gb300 import _lib
 
