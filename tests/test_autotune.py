@@ -1,7 +1,6 @@
 """Launch-configuration table (CPU: the table itself) and the autotuner (GPU)."""
 import json
 
-import numpy as np
 import pytest
 
 from matrixinversion_gb300 import _lib, autotune

@@ -8,8 +8,6 @@ import zlib
 import numpy as np
 import pytest
 
-from oracle import oracle as O
-
 
 def test_mt19937_stream_matches_numpy(oracle):
     # MT19937(seed 0) first outputs, and the float mapping, against numpy's
