@@ -185,3 +185,57 @@ def test_logical_positions_reproduce_getrf_pivots_with_ties():
             assert got == want, (A.tolist(), got, want)
             tie_steps += ties
     assert tie_steps > 300            # ties are what this checks
+
+
+def _gauss_jordan_slots(A, win):
+    """The kernels' elimination in FP64, batched: rows stay in their slots;
+    step k pivots on slot win[b][k] and column k.  Every other row takes
+    a -= (a[k] / pivot) * w, with w the unscaled pivot row whose entry k is
+    replaced by 1; column k itself becomes the identity column (1 in the
+    pivot row, -multiplier elsewhere).  After n steps each row is scaled by
+    1 / (the pivot of the step that chose it) and stored at output row
+    omap[slot] with columns permuted: A^-1[omap[s]][win[j]] = X[s][j]."""
+    B, n, _ = A.shape
+    X = A.astype(np.float64).copy()
+    rows = np.arange(B)
+    d = np.empty((B, n))
+    for k in range(n):
+        r = win[:, k]
+        piv = X[rows, r, k].copy()
+        w = X[rows, r, :].copy()
+        w[:, k] = 1.0
+        c = X[:, :, k].copy()
+        c[rows, r] = 0.0
+        X[:, :, k] = 0.0
+        X[rows, r, k] = 1.0
+        X -= (c / piv[:, None])[:, :, None] * w[:, None, :]
+        d[:, k] = piv
+    omap = np.empty_like(win)
+    omap[rows[:, None], win] = np.arange(n)[None, :]
+    X /= np.take_along_axis(d, omap, axis=1)[:, :, None]
+    out = np.empty_like(X)
+    out[rows[:, None, None], omap[:, :, None], win[:, None, :]] = X
+    return out
+
+
+@pytest.mark.parametrize("n", [2, 5, 16, 17, 32])
+def test_gauss_jordan_forms_of_the_kernels_invert(oracle, n):
+    """Both forms the CUDA kernels use give A^-1 (FP64, against numpy):
+    the lane-group form loads rows in pivot order and pivots on the diagonal
+    (win = identity), writing columns through the permutation; the slot form
+    (partial pivoting) leaves rows in place and permutes rows and columns at
+    the store."""
+    A = oracle.uniform(700 + n, 200, n)
+    inv = np.linalg.inv(A.astype(np.float64))
+    tol = 1e-9 * np.abs(inv).max(axis=(1, 2))
+    # lane-group form: the reference rule's pivots, rows loaded in pivot order
+    perm = oracle.pivots(A, "reference")
+    ident = np.tile(np.arange(n), (A.shape[0], 1))
+    Xb = _gauss_jordan_slots(np.take_along_axis(A, perm[:, :, None], axis=1), ident)
+    got = np.empty_like(Xb)
+    got[np.arange(A.shape[0])[:, None, None], np.arange(n)[None, :, None], perm[:, None, :]] = Xb
+    assert np.all(np.abs(got - inv).max(axis=(1, 2)) <= tol)
+    # slot form: partial pivoting's row order, rows never moved
+    _, p64, _ = oracle.inverse_f64(A, "partial")
+    got = _gauss_jordan_slots(A, p64.astype(np.int64))
+    assert np.all(np.abs(got - inv).max(axis=(1, 2)) <= tol)
