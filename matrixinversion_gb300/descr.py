@@ -77,6 +77,17 @@ def batched_inverse_descr_(packed, offsets, ns, flags, *, perm=None, info=None, 
     if ns.numel() != count or flags.numel() != count:
         raise ValueError("offsets, ns and flags must have the same length")
     dev = packed.device
+    for name, t in (("offsets", offsets), ("ns", ns), ("flags", flags)):
+        if t.device != dev:
+            raise ValueError(f"{name} must be on {dev}, with packed")
+    # the kernels write perm[i * 32 ..] and info[i] for every listed matrix
+    for name, t, numel in (("perm", perm, count * 32), ("info", info, count)):
+        if t is not None and not (isinstance(t, torch.Tensor) and t.is_cuda and t.dtype == torch.int32
+                                  and t.is_contiguous() and t.device == dev and t.numel() == numel):
+            raise ValueError(f"{name} must be a contiguous int32 tensor of {numel} elements on {dev}")
+    if workspace is not None and not (isinstance(workspace, torch.Tensor) and workspace.device == dev
+                                      and workspace.is_contiguous()):
+        raise ValueError(f"workspace must be a contiguous tensor on {dev}")
     if workspace is None:
         workspace = torch.empty(max(workspace_bytes(count), 256), dtype=torch.uint8, device=dev)
     L = _lib.load()
@@ -86,7 +97,8 @@ def batched_inverse_descr_(packed, offsets, ns, flags, *, perm=None, info=None, 
             ctypes.c_void_p(packed.data_ptr()), ctypes.c_void_p(offsets.data_ptr()), ctypes.c_void_p(ns.data_ptr()),
             ctypes.c_void_p(flags.data_ptr()), ctypes.c_void_p(perm.data_ptr() if perm is not None else 0),
             ctypes.c_void_p(info.data_ptr() if info is not None else 0), count, n_mask & 0xFFFFFFFF,
-            mode_mask & 0xF, ctypes.c_void_p(workspace.data_ptr()), workspace.numel(), ctypes.c_void_p(st))
+            mode_mask & 0xF, ctypes.c_void_p(workspace.data_ptr()), workspace.numel() * workspace.element_size(),
+            ctypes.c_void_p(st))
     _lib.check(status)
     return perm, info
 
