@@ -30,6 +30,28 @@ REFINE_FLAG = 8.0
 REFINE_TOL = 3e-7
 
 
+def _check_pair(A, X, max_n: int = 32):
+    """A and X: contiguous CUDA float32 [batch, n, n] of one shape on one
+    device (the kernels index both by the same batch position)."""
+    import torch
+
+    for name, t in (("A", A), ("X", X)):
+        if not (isinstance(t, torch.Tensor) and t.is_cuda and t.dtype == torch.float32 and t.is_contiguous()):
+            raise TypeError(f"{name} must be a contiguous CUDA float32 tensor")
+    if A.shape != X.shape or A.device != X.device or A.dim() != 3 or A.shape[-1] != A.shape[-2] \
+            or not 1 <= A.shape[-1] <= max_n:
+        raise ValueError(f"A and X must both be [batch, n, n] with n <= {max_n}, on one device")
+
+
+def _check_list(name, t, device, numel=None):
+    import torch
+
+    if not (isinstance(t, torch.Tensor) and t.is_cuda and t.dtype == torch.int32 and t.is_contiguous()
+            and t.device == device and (numel is None or t.numel() == numel)):
+        what = f" of {numel} entries" if numel is not None else ""
+        raise TypeError(f"{name} must be a contiguous CUDA int32 tensor{what} on {device}")
+
+
 def newton_schulz_(A, X, steps: int = 1, stream=None):
     """Refine X (in place) toward A^-1: X <- X + X (I - A X), `steps` times.
     A, X: contiguous CUDA float32 [batch, 32, 32]."""
@@ -53,8 +75,8 @@ def refine_fp64_(A, X, index, stream=None):
     index: CUDA int32 tensor of batch indices."""
     import torch
 
-    if not (index.is_cuda and index.dtype == torch.int32 and index.is_contiguous()):
-        raise TypeError("index must be a contiguous CUDA int32 tensor")
+    _check_pair(A, X)
+    _check_list("index", index, A.device)
     n = A.shape[-1]
     st = (stream or torch.cuda.current_stream(A.device)).cuda_stream
     with torch.cuda.device(A.device):
@@ -76,8 +98,8 @@ def refine_df_(A, X, index, stream=None, next_tol=None, next_out=None):
     be `index` itself."""
     import torch
 
-    if not (index.is_cuda and index.dtype == torch.int32 and index.is_contiguous()):
-        raise TypeError("index must be a contiguous CUDA int32 tensor")
+    _check_pair(A, X)
+    _check_list("index", index, A.device)
     n = A.shape[-1]
     st = (stream or torch.cuda.current_stream(A.device)).cuda_stream
     lib = _lib.load()
@@ -90,9 +112,7 @@ def refine_df_(A, X, index, stream=None, next_tol=None, next_out=None):
             return X
         if next_out is None:
             next_out = torch.empty_like(index)
-        if not (next_out.is_cuda and next_out.dtype == torch.int32 and next_out.is_contiguous()
-                and next_out.numel() == index.numel()):
-            raise TypeError("next_out must be a contiguous CUDA int32 tensor shaped like index")
+        _check_list("next_out", next_out, A.device, index.numel())
         status = lib.mi_refine_df_next_f32(ctypes.c_void_p(A.data_ptr()), ctypes.c_void_p(X.data_ptr()),
                                            ctypes.c_void_p(index.data_ptr()), index.numel(), A.shape[0], n,
                                            float(next_tol), ctypes.c_void_p(next_out.data_ptr()),
@@ -119,9 +139,11 @@ def flag_list(A, X, threshold: float = 1e4, out=None):
     refine_df_ / refine_fp64_ take it as it is."""
     import torch
 
+    _check_pair(A, X)
     batch, n = A.shape[0], A.shape[-1]
     if out is None:
         out = torch.empty(batch, dtype=torch.int32, device=A.device)
+    _check_list("out", out, A.device, batch)
     st = torch.cuda.current_stream(A.device).cuda_stream
     with torch.cuda.device(A.device):
         status = _lib.load().mi_flag_condition_f32(ctypes.c_void_p(A.data_ptr()), ctypes.c_void_p(X.data_ptr()),

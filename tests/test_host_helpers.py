@@ -130,3 +130,21 @@ def test_reference_arm_line(capsys):
     bench.run_reference_arm(args, rank=1)              # other ranks print nothing
     assert capsys.readouterr().out == ""
     assert bench.algorithmic_bytes(32) == 8324
+
+
+def test_wrappers_reject_host_tensors_before_any_call():
+    """The refinement and descriptor wrappers take device tensors only: a host
+    tensor is an error before the library is called (there is no host path)."""
+    import torch
+
+    from matrixinversion_gb300 import descr, refine
+
+    A = torch.zeros(2, 32, 32)
+    idx = torch.zeros(2, dtype=torch.int32)
+    for call in (lambda: refine.newton_schulz_(A, A.clone()), lambda: refine.refine_fp64_(A, A.clone(), idx),
+                 lambda: refine.refine_df_(A, A.clone(), idx), lambda: refine.flag_list(A, A.clone()),
+                 lambda: descr.batched_inverse_descr_(torch.zeros(16), torch.zeros(1, dtype=torch.int64),
+                                                      torch.ones(1, dtype=torch.int32),
+                                                      torch.ones(1, dtype=torch.int32))):
+        with pytest.raises(TypeError):
+            call()
