@@ -239,3 +239,147 @@ def test_gauss_jordan_forms_of_the_kernels_invert(oracle, n):
     _, p64, _ = oracle.inverse_f64(A, "partial")
     got = _gauss_jordan_slots(A, p64.astype(np.int64))
     assert np.all(np.abs(got - inv).max(axis=(1, 2)) <= tol)
+
+
+# ---------------------------------------------------------------------------
+# The kernels' fast replays of the reference pivot rules, restated on the CPU.
+# Safety property: whenever a fast replay does not flag a matrix (tie or NaN),
+# its pivot order equals the exact rule's (the oracle, itself pinned to the
+# reference kernels); flagged matrices are replayed exactly on the GPU.
+# ---------------------------------------------------------------------------
+
+def _fast_key(A):
+    """max.NaN.ftz(|x|, 0) as bits: subnormals and zeros 0, NaN 0x7fffffff."""
+    b = A.view(np.uint32) & np.uint32(0x7FFFFFFF)
+    b = np.where(b < 0x00800000, np.uint32(0), b)
+    return np.where(b > 0x7F800000, np.uint32(0x7FFFFFFF), b).astype(np.uint64)
+
+
+def _survive_mask(T):
+    m = 0
+    for t in range(T):
+        p, alive, s = t, True, T // 2
+        while s > 0:
+            if p >= 2 * s:
+                alive = False
+                break
+            if p >= s:
+                p -= s
+            s //= 2
+        if alive and p == 0:
+            m |= 1 << t
+    return m
+
+
+def _lanes(n):
+    return 4 if n <= 4 else 8 if n <= 8 else 16 if n <= 16 else 32
+
+
+def _win_from(final, bad, n):
+    win = np.full((final.shape[0], n), -1, dtype=np.int64)
+    ok = ~bad
+    b = np.nonzero(ok)[0]
+    win[b[:, None], final[ok, :n]] = np.arange(n)[None, :]
+    return win
+
+
+def _dup(final, n):
+    srt = np.sort(final[:, :n], axis=1)
+    return (srt[:, 1:] == srt[:, :-1]).any(axis=1) if n > 1 else np.zeros(final.shape[0], bool)
+
+
+def _replay_fast(A):
+    """replay_fast_multi: per step the group maximum of the keys of the rows
+    not yet placed; every lane holding it takes the step.  Flag: two rows on
+    one step, or a NaN key in some maximum."""
+    B, n, _ = A.shape
+    P = _lanes(n)
+    keys = np.zeros((B, P, n), dtype=np.uint64)
+    keys[:, :n, :] = _fast_key(A)
+    placed = np.zeros((B, P), dtype=bool)
+    placed[:, n:] = True
+    step = np.zeros((B, P), dtype=np.int64)
+    top = np.zeros(B, dtype=np.uint64)
+    for k in range(n):
+        cand = np.where(placed, 0, keys[:, :, k])
+        mx = cand.max(axis=1)
+        top = np.maximum(top, mx)
+        hit = cand == mx[:, None]
+        placed |= hit
+        step = np.where(hit, k, step)
+    bad = _dup(step, n) | (top > 0x7F800000)
+    return _win_from(step, bad, n), bad
+
+
+def _replay_tracked(A):
+    """replay_tracked_multi: positions tracked; key 2|x| for a candidate whose
+    tree slot survives, 2|x| + 1 for the row on the diagonal; an odd maximum
+    keeps the diagonal, an even one names the winner, whose old position goes
+    to the displaced row.  Flag: two rows on one final position, or a NaN."""
+    B, n, _ = A.shape
+    P = _lanes(n)
+    ksurv = _survive_mask(n)
+    ek = np.zeros((B, P, n), dtype=np.uint64)
+    ek[:, :n, :] = _fast_key(A) << np.uint64(1)
+    pos = np.tile(np.concatenate([np.arange(n), np.full(P - n, 31)]), (B, 1)).astype(np.int64)
+    top = np.zeros(B, dtype=np.uint64)
+    rows = np.arange(B)
+    for k in range(n):
+        surv = (ksurv << (k + 1)) & 0xFFFFFFFF if k + 1 < 32 else 0
+        at = pos == k
+        live = ((surv >> pos) & 1).astype(bool)
+        e = np.where(at, ek[:, :, k] | np.uint64(1), np.where(live, ek[:, :, k], np.uint64(0)))
+        mx = e.max(axis=1)
+        top = np.maximum(top, mx)
+        hit = ~at & (e == mx[:, None])
+        if P == 32:
+            wpos = np.where(hit, pos, 0).max(axis=1)
+        else:
+            wpos = pos[rows, np.argmax(hit, axis=1)]
+        keep = (mx & np.uint64(1)) == 0
+        pos = np.where(hit, k, np.where(at & keep[:, None], wpos[:, None], pos))
+    bad = _dup(pos, n) | (top > (0x7F800000 << 1) + 1)
+    return _win_from(pos, bad, n), bad
+
+
+def _replay_inputs(oracle, n, seed):
+    """Uniform matrices, and harder ones: small integers (ties everywhere),
+    uniform matrices with a few special entries each (zero, a subnormal that
+    compares as 0, +-inf; NaN in one matrix of eight), and uniform matrices
+    with equal-magnitude pairs planted in random columns (ties that decide a
+    step only when they hold the maximum)."""
+    rng = np.random.RandomState(seed)
+    uni = oracle.uniform(seed, 256, n)
+    ties = rng.randint(-3, 4, size=(64, n, n)).astype(np.float32)
+    spec = oracle.uniform(seed + 1, 256, n)
+    for b in range(spec.shape[0]):
+        for _ in range(rng.randint(1, 4)):
+            i, j = rng.randint(0, n, size=2)
+            spec[b, i, j] = rng.choice(np.array([0.0, 3e-39, -2e-39, np.inf, -np.inf], dtype=np.float32))
+        if b % 8 == 0:
+            i, j = rng.randint(0, n, size=2)
+            spec[b, i, j] = np.nan
+    pairs = oracle.uniform(seed + 2, 256, n)
+    for b in range(pairs.shape[0]):
+        for _ in range(rng.randint(1, 4)):
+            j = rng.randint(0, n)
+            i0, i1 = rng.randint(0, n, size=2)
+            pairs[b, i1, j] = np.float32(rng.choice([-1.0, 1.0])) * pairs[b, i0, j]
+    return uni, np.concatenate([ties, spec, pairs])
+
+
+@pytest.mark.parametrize("n", range(1, 33))
+def test_fast_replays_agree_with_the_exact_rule_unless_flagged(oracle, n):
+    uni, hard = _replay_inputs(oracle, n, 9100 + n)
+    cases = [("reference_serial", _replay_fast)]
+    cases.append(("reference", _replay_fast if (n & (n - 1)) == 0 else _replay_tracked))
+    for mode, replay in cases:
+        for A in (uni, hard):
+            win, bad = replay(A)
+            want = oracle.pivots(A, mode)
+            ok = ~bad
+            assert np.array_equal(win[ok], want[ok]), (mode, np.nonzero((win != want).any(1) & ok)[0][:5])
+        # ordinary inputs take the fast path (a tie among random floats is
+        # rare), and most of the hard ones are checked rather than flagged
+        assert replay(uni)[1].mean() <= 0.02, mode
+        assert (~replay(hard)[1]).sum() >= 0.4 * (hard.shape[0] - 64), mode
