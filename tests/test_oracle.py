@@ -383,3 +383,81 @@ def test_fast_replays_agree_with_the_exact_rule_unless_flagged(oracle, n):
         # rare), and most of the hard ones are checked rather than flagged
         assert replay(uni)[1].mean() <= 0.02, mode
         assert (~replay(hard)[1]).sum() >= 0.4 * (hard.shape[0] - 64), mode
+
+
+def _pivot_key(A):
+    """Exact key: |x| bits, subnormals 0, NaN 0xffffffff (never a candidate)."""
+    b = A.view(np.uint32) & np.uint32(0x7FFFFFFF)
+    b = np.where(b < 0x00800000, np.uint32(0), b)
+    return np.where(b > 0x7F800000, np.uint32(0xFFFFFFFF), b).astype(np.uint64)
+
+
+def _prio(T):
+    """Tie rank of each tree slot (higher wins, 0 = dropped): run the tree on
+    tie-only inputs, taking out the winner each round."""
+    alive = [t < T for t in range(32)]
+    rank_of = [0] * 32
+    for rank in range(32, 0, -1):
+        val = [1 if alive[t] else 0 for t in range(32)]
+        idx = list(range(32))
+        s = T // 2
+        while s > 0:
+            for t in range(s):
+                if val[t] < val[t + s]:
+                    val[t], idx[t] = val[t + s], idx[t + s]
+            s //= 2
+        if val[0] == 0:
+            break
+        rank_of[idx[0]] = rank
+        alive[idx[0]] = False
+    return np.array(rank_of, dtype=np.int64)
+
+
+def _replay_exact(A, mode):
+    """exact_pivot / replay_tracked: positions tracked step by step; a
+    candidate must beat the diagonal strictly and not be NaN, and (reference
+    rule) sit in a surviving tree slot; ties go to the tree's slot priority
+    (reference) or the lowest position (serial); if nothing qualifies the
+    diagonal stays."""
+    B, n, _ = A.shape
+    key = _pivot_key(A)
+    pos = np.tile(np.arange(n), (B, 1)).astype(np.int64)
+    lanes = np.arange(n)[None, :]
+    rows = np.arange(B)
+    ksurv, prio = _survive_mask(n), _prio(n)
+    win = np.zeros((B, n), dtype=np.int64)
+    for k in range(n):
+        kraw = key[:, :, k]
+        dl = np.argmax(pos == k, axis=1)
+        kd = kraw[rows, dl]
+        slot = pos - k - 1
+        ok = (slot >= 0) & (kraw > kd[:, None]) & (kraw <= 0x7F800000)
+        sc = np.clip(slot, 0, 31)
+        if mode == "reference":
+            ok &= ((ksurv >> sc) & 1).astype(bool)
+        cand = np.where(ok, kraw, 0)
+        top = ok & (cand == cand.max(axis=1)[:, None])
+        pr = np.where(top, prio[sc] if mode == "reference" else 64 - pos, 0)
+        sel = top & (pr == pr.max(axis=1)[:, None])
+        wl = np.where(sel.any(axis=1), np.argmax(sel, axis=1), dl)
+        pw = pos[rows, wl]
+        pos = np.where(lanes == wl[:, None], k, np.where(pos == k, pw[:, None], pos))
+        win[:, k] = wl
+    return win
+
+
+@pytest.mark.parametrize("n", range(1, 33))
+def test_exact_replay_matches_the_reference_rule_on_every_input(oracle, golden, n):
+    uni, hard = _replay_inputs(oracle, n, 9300 + n)
+    ties = golden[f"n{n}_ties_A"].astype(np.float32) if f"n{n}_ties_A" in golden else hard[:0]
+    for mode in ("reference", "reference_serial"):
+        for A in (uni, hard, ties):
+            got = _replay_exact(A, mode)
+            want = oracle.pivots(A, mode)
+            bad = np.nonzero((got != want).any(axis=1))[0]
+            assert bad.size == 0, (mode, bad[:5])
+    # and straight against the pivots the reference kernels produced
+    for kind in ("ties", "nan"):
+        A = golden[f"n{n}_{kind}_A"].astype(np.float32)
+        assert np.array_equal(_replay_exact(A, "reference"), golden[f"n{n}_{kind}_piv_parallel"])
+        assert np.array_equal(_replay_exact(A, "reference_serial"), golden[f"n{n}_{kind}_piv_serial"])
