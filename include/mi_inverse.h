@@ -201,6 +201,8 @@ int mi_newton_schulz_f32(const float* d_a, float* d_x, int64_t batch, int n, int
  * and X <- X + X R evaluated in FP64, X rounded once to FP32.  For the
  * matrices a cheap test flags as ill-conditioned, where an FP32 residual is
  * no better than the inverse itself.  Out-of-range list entries are skipped.
+ * No counterpart in the reference, which computes in FP32 only (its FP64
+ * switch is commented out, parallel_pivot/verify.hpp:9).
  */
 int mi_refine_fp64_f32(const float* d_a, float* d_x, const int32_t* d_list, int64_t count, int64_t batch, int n,
                        void* stream);
@@ -210,7 +212,7 @@ int mi_refine_fp64_f32(const float* d_a, float* d_x, const int32_t* d_list, int6
  * float-float arithmetic on the FP32 pipes (exact products, TwoSum
  * accumulation: about 44 significant bits) and X R in FP32 -- the same
  * accuracy gain where kappa * u < 1, several times faster on GPUs whose FP64
- * rate is low.
+ * rate is low.  No counterpart in the reference.
  */
 int mi_refine_df_f32(const float* d_a, float* d_x, const int32_t* d_list, int64_t count, int64_t batch, int n,
                      void* stream);
@@ -231,7 +233,8 @@ int mi_refine_df_next_f32(const float* d_a, float* d_x, const int32_t* d_list, i
  * d_list[b] = b if ||A_b||_1 * ||X_b||_1 >= threshold (or is not finite),
  * else -1, for b in [0, batch): a list the two refinement calls take as it is
  * (count = batch; -1 entries are skipped), so flagging needs no host round
- * trip.
+ * trip.  No counterpart in the reference (its host code computes a condition
+ * number only for reporting, parallel_pivot/verify.hpp:246-338).
  */
 int mi_flag_condition_f32(const float* d_a, const float* d_x, int64_t batch, int n, float threshold,
                           int32_t* d_list, void* stream);
@@ -247,6 +250,9 @@ int mi_get_launch_config(int n, int pivot, int* threads_per_block);
 const char* mi_error_string(int status);
 /* Text of the last CUDA error seen by this thread ("" if none). */
 const char* mi_last_cuda_error(void);
+/* MI_ABI_VERSION of the loaded library, to check against the header a
+   caller was built with (no counterpart in the reference, which has no
+   library). */
 int mi_abi_version(void);
 
 #ifdef __cplusplus
