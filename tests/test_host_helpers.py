@@ -148,3 +148,35 @@ def test_wrappers_reject_host_tensors_before_any_call():
                                                       torch.ones(1, dtype=torch.int32))):
         with pytest.raises(TypeError):
             call()
+
+
+def test_residual_reports():
+    """The sweep's residual statistics and the serving loop's residual check,
+    on host tensors: exact inverses give ~0, a perturbed one is counted."""
+    import torch
+
+    from matrixinversion_gb300 import serving, sweep
+
+    A = torch.from_numpy(np.linalg.qr(np.random.RandomState(4).randn(64, 8, 8))[0]).float()  # orthogonal
+    X = A.transpose(1, 2).contiguous()
+    X[5, 0, 0] += 0.01                                   # one matrix off by 1e-2 in one entry
+    st = sweep.residual_stats(A, X, sample=64)
+    assert st["median"] < 1e-5 and st["max"] > 5e-3
+    assert abs(st["fail_1e-3"] - 1 / 64) < 1e-9           # verifyInv's criterion fails for exactly one
+    r = serving.residual_max(A.numpy(), X.numpy())
+    assert abs(r - st["max"]) < 1e-6
+
+
+def test_condition_flags_on_host_tensors():
+    """flag_ill_conditioned: ||A||_1 ||X||_1 >= threshold, or not finite."""
+    import torch
+
+    from matrixinversion_gb300 import refine
+
+    A = torch.eye(4).repeat(3, 1, 1)
+    X = torch.eye(4).repeat(3, 1, 1)
+    X[1] *= 1e5                                          # estimate 1e5
+    X[2, 0, 0] = float("nan")                            # not finite
+    idx = refine.flag_ill_conditioned(A, X, threshold=1e4)
+    assert idx.dtype == torch.int32 and idx.tolist() == [1, 2]
+    assert refine.flag_ill_conditioned(A, X, threshold=1e6).tolist() == [2]
