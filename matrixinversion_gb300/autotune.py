@@ -57,7 +57,7 @@ def tune(ns=range(1, 33), modes=("none", "reference"), batch: int = 262144, iter
     import matrixinversion_gb300 as mi
 
     table = {}
-    g = torch.Generator(device="cuda").manual_seed(seed)
+    g = None                          # made on the first size that is timed
     for n in ns:
         tunable = [m for m in modes if mi.query_launch(n, m, batch)["knob"]]
         for m in modes:
@@ -65,6 +65,8 @@ def tune(ns=range(1, 33), modes=("none", "reference"), batch: int = 262144, iter
                 table[(n, m)] = {"best": 0, "ms": {}, "form": mi.query_launch(n, m, batch)["form"]}
         if not tunable:
             continue
+        if g is None:
+            g = torch.Generator(device="cuda").manual_seed(seed)
         src = torch.rand(batch, n, n, generator=g, device="cuda") * 2 - 1
         work = torch.empty_like(src)
         for mode in tunable:

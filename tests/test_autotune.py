@@ -61,3 +61,14 @@ def test_tuning_installs_best_and_keeps_results(mi_gpu, oracle):
     X, _, _ = mi_gpu.batched_inverse(A, "reference")
     assert torch.equal(X, ref)
     autotune.set_config(20, "reference", 0)
+
+
+def test_fixed_block_sizes_are_reported_not_timed(lib):
+    """Sizes whose contiguous launch has a fixed block are skipped without
+    touching a device: nothing is timed or installed for them."""
+    before = {(n, m): autotune.get_config(n, m) for n in (1, 8, 16) for m in ("none", "reference", "partial")}
+    table = autotune.tune([1, 8], ["none", "reference"], batch=4096)
+    assert table == {(n, m): {"best": 0, "ms": {}, "form": "thread"} for n in (1, 8) for m in ("none", "reference")}
+    table = autotune.tune([16], ["partial"], batch=4096)
+    assert table == {(16, "partial"): {"best": 0, "ms": {}, "form": "rows"}}
+    assert {(n, m): autotune.get_config(n, m) for n in (1, 8, 16) for m in ("none", "reference", "partial")} == before
