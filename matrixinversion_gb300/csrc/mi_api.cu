@@ -76,7 +76,7 @@ static const int kTunedGB300[33][4] = {
     {128, 256, 256, 256},
     {64, 256, 256, 256},
     {64, 64, 64, 256},
-    {128, 128, 128, 256}};
+    {256, 256, 256, 256}};
 static int g_tuned[33][4];
 static bool g_tuned_init = [] {
     for (int n = 0; n < 33; n++)
@@ -138,6 +138,12 @@ static void geom_of(int& lanes, int& mpw, int& smem_warp) {
         // staged through shared memory unless each thread moves its matrix
         // with 16-byte copies
         smem_warp = ((N * N) % 4 == 0 && N < kTinySlotMin) ? 0 : 32 * tiny_pitch<N>() * 4;
+        return;
+    }
+    if constexpr (N == WideGeom::N) {                           // eight lanes, 16 x 8 register blocks
+        lanes = WideGeom::L;
+        mpw = WideGeom::M;
+        smem_warp = WideGeom::kWarp * 4;
         return;
     }
     constexpr int L = default_lanes(N, kModeReference);

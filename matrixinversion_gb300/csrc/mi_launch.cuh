@@ -25,6 +25,7 @@ PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder();  // driver entry point (
 
 #include "mi_tiny.cuh"
 #include "mi_rows.cuh"
+#include "mi_wide.cuh"
 
 namespace mi {
 
@@ -44,16 +45,86 @@ inline bool make_tensor_map(CUtensorMap* map, float* a, int n, long long batch, 
     return r == CUDA_SUCCESS;
 }
 
-template <int N, int MODE>
-cudaError_t launch(float* a, int32_t* perm, int32_t* info, long long batch, int tpb, int grid,
-                   cudaStream_t stream) {
-    if constexpr (N <= kTinyMax) {
-        return launch_tiny<N, MODE>(a, perm, info, batch, tpb, grid, stream);
-    } else if constexpr (N <= tiny_max_contig<MODE>()) {
-        if (batch >= tiny_min_batch<N, MODE>()) return launch_tiny<N, MODE>(a, perm, info, batch, tpb, grid, stream);
+// n = 32 without partial pivoting: the eight-lane form (mi_wide.cuh), with
+// tensor copies.  Sets *used = false, launching nothing, when the batch does
+// not allow them (pointer not 16-byte aligned, more than 2^31 - 1 matrices).
+template <int MODE>
+cudaError_t launch_wide(float* a, int32_t* perm, int32_t* info, long long batch, int tpb, int grid,
+                        cudaStream_t stream, bool* used) {
+    using G = WideGeom;
+    *used = false;
+    CUtensorMap map, map_out;
+    std::memset(&map, 0, sizeof(map));
+    std::memset(&map_out, 0, sizeof(map_out));
+    if ((reinterpret_cast<uintptr_t>(a) & 15u) != 0 || batch > 0x7fffffffLL ||
+        !make_tensor_map(&map, a, G::N, batch, G::N, G::M) || !make_tensor_map(&map_out, a, G::N, batch, G::ORows, G::M))
+        return cudaSuccess;
+    *used = true;
+    if (tpb > G::kThreadsMax) tpb = G::kThreadsMax;
+    const int warps = tpb / 32;
+    const size_t smem = wide_smem_bytes(warps);
+    auto kern = mi_wide_kernel<MODE>;
+    static size_t smem_set[kMaxDevices] = {};
+    {
+        const cudaError_t e = opt_in_smem(kern, smem, smem_set);
+        if (e != cudaSuccess) return e;
     }
-    if constexpr (MODE == kModePartial && N >= kRowsMin && rows_partial_enabled<N>())
-        return launch_rows_partial<N>(a, perm, info, batch, grid, stream);
+    const long long groups = (batch + G::M - 1) / G::M;
+    const long long need = (groups + warps - 1) / warps;
+    if (grid <= 0) {
+        int per_sm = 0;
+        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, tpb, smem);
+        if (e != cudaSuccess) return e;
+        if (per_sm < 1) per_sm = 1;
+        const long long cap = (long long)per_sm * device_sm_count();
+        grid = (int)(need < cap ? need : cap);
+    }
+    if (grid < 1) grid = 1;
+    kern<<<grid, tpb, smem, stream>>>(a, perm, info, batch, map, map_out);
+    return cudaGetLastError();
+}
+
+// The eight-lane form for descriptor buckets (IDX) and for contiguous batches
+// the tensor copies cannot take (matrix b at a + 1024 b).
+template <int MODE, bool IDX>
+cudaError_t launch_wide_gather(float* a, const long long* offsets, const int* list, const long long* range,
+                               long long batch, int32_t* perm, int32_t* info, int tpb, int grid,
+                               cudaStream_t stream) {
+    using G = WideGeom;
+    if (tpb > G::kThreadsMax) tpb = G::kThreadsMax;
+    const int warps = tpb / 32;
+    const size_t smem = wide_smem_bytes(warps);
+    auto kern = mi_wide_gather_kernel<MODE, IDX>;
+    static size_t smem_set[kMaxDevices] = {};
+    {
+        const cudaError_t e = opt_in_smem(kern, smem, smem_set);
+        if (e != cudaSuccess) return e;
+    }
+    if (grid <= 0) {
+        static int per_sm_cached[kMaxDevices][G::kThreadsMax / 32 + 1] = {};
+        int dev = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) dev = 0;
+        int& per_sm = per_sm_cached[dev][warps];
+        if (per_sm == 0) {
+            cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, tpb, smem);
+            if (e != cudaSuccess) return e;
+            if (per_sm < 1) per_sm = 1;
+        }
+        long long cap = (long long)per_sm * device_sm_count();
+        if (!IDX) {
+            const long long need = ((batch + G::M - 1) / G::M + warps - 1) / warps;
+            if (need < cap) cap = need;
+        }
+        grid = (int)(cap < 1 ? 1 : cap);
+    }
+    kern<<<grid, tpb, smem, stream>>>(a, offsets, list, range, batch, perm, info);
+    return cudaGetLastError();
+}
+
+// The lane-group kernel (mi_inverse_kernel) for a contiguous batch.
+template <int N, int MODE>
+cudaError_t launch_lanes(float* a, int32_t* perm, int32_t* info, long long batch, int tpb, int grid,
+                         cudaStream_t stream) {
     constexpr int L = default_lanes(N, MODE);
     using G = Geom<N, L>;
     const int warps = tpb / 32;
@@ -101,6 +172,28 @@ cudaError_t launch(float* a, int32_t* perm, int32_t* info, long long batch, int 
     return cudaGetLastError();
 }
 
+template <int N, int MODE>
+cudaError_t launch(float* a, int32_t* perm, int32_t* info, long long batch, int tpb, int grid,
+                   cudaStream_t stream) {
+    if constexpr (N == WideGeom::N && MODE != kModePartial) {
+        bool used = false;
+        const cudaError_t e = launch_wide<MODE>(a, perm, info, batch, tpb, grid, stream, &used);
+        if (used) return e;
+        return launch_wide_gather<MODE, false>(a, nullptr, nullptr, nullptr, batch, perm, info, tpb, grid, stream);
+    } else {
+        if constexpr (N <= kTinyMax) {
+            return launch_tiny<N, MODE>(a, perm, info, batch, tpb, grid, stream);
+        } else if constexpr (N <= tiny_max_contig<MODE>()) {
+            if (batch >= tiny_min_batch<N, MODE>())
+                return launch_tiny<N, MODE>(a, perm, info, batch, tpb, grid, stream);
+        }
+        if constexpr (MODE == kModePartial && N >= kRowsMin && rows_partial_enabled<N>())
+            return launch_rows_partial<N>(a, perm, info, batch, grid, stream);
+        else
+            return launch_lanes<N, MODE>(a, perm, info, batch, tpb, grid, stream);
+    }
+}
+
 // What launch<N, MODE> runs for a contiguous batch: the kernel form (the
 // MI_FORM_* codes of mi_inverse.h), lanes per matrix, matrices per warp and
 // threads per block.  The branches are launch<N, MODE>'s, in its order; only
@@ -121,6 +214,8 @@ LaunchForm launch_form(long long batch, int tpb) {
     }
     if constexpr (MODE == kModePartial && N >= kRowsMin && rows_partial_enabled<N>())
         return {kFormRows, kRowsLanes, kRowsMats, 32 * kRowsWarps};
+    if constexpr (N == WideGeom::N && MODE != kModePartial)
+        return {kFormLanes, WideGeom::L, WideGeom::M, tpb < WideGeom::kThreadsMax ? tpb : WideGeom::kThreadsMax};
     constexpr int L = default_lanes(N, MODE);
     return {kFormLanes, L, Geom<N, L>::M, tpb};
 }
@@ -136,6 +231,8 @@ cudaError_t launch_indexed(float* base, const long long* offsets, const int* lis
                            int32_t* perm, int32_t* info, int tpb, int grid, cudaStream_t stream) {
     if constexpr (N <= tiny_max_indexed<MODE>())
         return launch_tiny_indexed<N, MODE>(base, offsets, list, range, perm, info, tpb, grid, stream);
+    if constexpr (N == WideGeom::N && MODE != kModePartial)
+        return launch_wide_gather<MODE, true>(base, offsets, list, range, 0, perm, info, tpb, grid, stream);
     constexpr int L = default_lanes(N, MODE);
     const int warps = tpb / 32;
     const size_t smem = smem_bytes<N, L, MODE>(warps);

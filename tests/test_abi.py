@@ -91,7 +91,7 @@ def test_query_and_errors_without_gpu(lib):
     # n = 2, where each thread moves its matrix with 16-byte copies; larger n:
     # lane groups
     for n, want, staged in ((1, 1, True), (2, 1, False), (4, 1, True), (5, 1, True), (8, 1, True), (12, 1, True),
-                            (15, 1, True), (16, 8, True), (17, 16, True), (32, 16, True)):
+                            (15, 1, True), (16, 8, True), (17, 16, True), (32, 8, True)):
         assert lib.mi_query_config(n, ctypes.byref(lanes), ctypes.byref(mpw), ctypes.byref(smem),
                                    ctypes.byref(tpb)) == 0
         assert lanes.value == want and mpw.value == 32 // want and (smem.value > 0) == staged, n
@@ -154,7 +154,9 @@ def test_query_launch_reports_the_form_each_call_runs(lib):
         assert q(n, "partial", 10**6, 64) == ("rows", 16, 2, 128, False), n
     for n in (29, 30, 31):
         assert q(n, "partial", 10**6, 64) == ("lanes", 32, 1, 64, True), n
-    assert q(32, "reference", 10**6, 128) == ("lanes", 16, 2, 128, True)
+    # n = 32 without partial pivoting: eight lanes per matrix, four matrices per warp
+    assert q(32, "reference", 10**6, 128) == ("lanes", 8, 4, 128, True)
+    assert q(32, "none", 10, 512) == ("lanes", 8, 4, 256, True)
     # argument errors
     for bad in ((0, 1, 10, 0), (33, 1, 10, 0), (8, 4, 10, 0), (8, -1, 10, 0), (8, 1, -1, 0), (8, 1, 10, -32)):
         assert lib.mi_query_launch(*bad, None, None, None, None) == _lib.MI_ERR_INVALID_VALUE, bad
