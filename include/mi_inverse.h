@@ -45,7 +45,7 @@
 extern "C" {
 #endif
 
-#define MI_ABI_VERSION 1
+#define MI_ABI_VERSION 2
 
 /* status codes */
 #define MI_OK 0
@@ -122,9 +122,11 @@ int mi_query_launch(int n, int pivot, int64_t batch, int threads_per_block, int*
 /*
  * Mixed sizes in one call.  Matrix i is n_i x n_i (1..32), row-major at
  * d_packed + d_offsets[i] (floats), pivot mode d_flags[i] (MI_PIVOT_*),
- * inverted in place.  d_perm (nullable) int32[count][32]: pivots of matrix i
- * at d_perm[i * 32 ..]; d_info (nullable) int32[count]: as mi_inverse_f32,
- * or -1 for a malformed descriptor (n or flag out of range; not processed).
+ * inverted in place.  packed_floats: the size of d_packed in floats; every
+ * matrix must lie in [0, packed_floats).  d_perm (nullable) int32[count][32]:
+ * pivots of matrix i at d_perm[i * 32 ..]; d_info (nullable) int32[count]: as
+ * mi_inverse_f32, or -1 for a malformed descriptor (n or flag out of range,
+ * or a matrix that is not inside d_packed; not processed, not touched).
  * n_mask: bit n-1 set if size n may occur (0 = all sizes); mode_mask: bit m
  * set if pivot mode m may occur (0 = all) -- buckets outside the masks are
  * not launched.  d_workspace: caller-owned device scratch of at least
@@ -132,9 +134,9 @@ int mi_query_launch(int n, int pivot, int64_t batch, int threads_per_block, int*
  * only stream-ordered work (no host synchronisation), so it can be captured
  * into a CUDA graph.
  */
-int mi_inverse_descr_f32(float* d_packed, const int64_t* d_offsets, const int32_t* d_n, const int32_t* d_flags,
-                         int32_t* d_perm, int32_t* d_info, int64_t count, uint32_t n_mask, uint32_t mode_mask,
-                         void* d_workspace, size_t workspace_bytes, void* stream);
+int mi_inverse_descr_f32(float* d_packed, int64_t packed_floats, const int64_t* d_offsets, const int32_t* d_n,
+                         const int32_t* d_flags, int32_t* d_perm, int32_t* d_info, int64_t count, uint32_t n_mask,
+                         uint32_t mode_mask, void* d_workspace, size_t workspace_bytes, void* stream);
 size_t mi_descr_workspace_bytes(int64_t count);
 
 /*
@@ -152,7 +154,10 @@ size_t mi_descr_workspace_bytes(int64_t count);
  *   First call on each device: looks up the scratch's device address
  *                 (cudaGetSymbolAddress, with that device current), which also
  *                 loads the library's device code there if needed.  Make that
- *                 first call before any stream capture begins.
+ *                 first call before any stream capture begins.  The address is
+ *                 kept per device and context: the first call in a new context
+ *                 on the device (after cudaDeviceReset) looks it up again, so
+ *                 make that one before any capture too.
  *   Zeroing:      the caller clears nothing; each call resets the scratch's
  *                 bucket counters on `stream` before use, and the rest of the
  *                 scratch is written before it is read.
@@ -163,9 +168,9 @@ size_t mi_descr_workspace_bytes(int64_t count);
  * Arguments, results and other status codes as mi_inverse_descr_f32.
  */
 #define MI_NOALLOC_MAX_COUNT 262144
-int mi_inverse_descr_noalloc_f32(float* d_packed, const int64_t* d_offsets, const int32_t* d_n,
-                                 const int32_t* d_flags, int32_t* d_perm, int32_t* d_info, int64_t count,
-                                 uint32_t n_mask, uint32_t mode_mask, void* stream);
+int mi_inverse_descr_noalloc_f32(float* d_packed, int64_t packed_floats, const int64_t* d_offsets,
+                                 const int32_t* d_n, const int32_t* d_flags, int32_t* d_perm, int32_t* d_info,
+                                 int64_t count, uint32_t n_mask, uint32_t mode_mask, void* stream);
 
 /*
  * Waits that ran out on the device (no counterpart in the reference, whose
@@ -184,6 +189,23 @@ int mi_inverse_descr_noalloc_f32(float* d_packed, const int64_t* d_offsets, cons
 #define MI_DEVERR_COPY_TIMEOUT 1
 #define MI_DEVERR_MMA_TIMEOUT 2
 int mi_device_error(int* flags, int clear);
+
+/*
+ * Test hook of the bounded waits (no counterpart in the reference): lets a
+ * test make a tile-copy wait run out without a fault or a stalled copy.
+ * wait_limit_cycles  the longest wait of the contiguous inverse kernels on
+ *                    a tile copy, in SM clocks (<= 0 restores the default of
+ *                    about two seconds);
+ * arm_without_copy   != 0: each warp arms its copy barrier with the bytes it
+ *                    expects but issues no copy, so every such wait runs out
+ *                    (nothing is in flight, nothing lands late); the warps
+ *                    then record MI_DEVERR_COPY_TIMEOUT and return with their
+ *                    matrices unwritten.
+ * Applies to later launches on the current device until reset with
+ * mi_set_wait_test(0, 0).  Not for production use: a call in test mode
+ * returns MI_OK and leaves its outputs unwritten.
+ */
+int mi_set_wait_test(int64_t wait_limit_cycles, int arm_without_copy);
 
 /*
  * Newton-Schulz refinement of n = 32 inverses on the tensor cores (no

@@ -62,16 +62,19 @@ def load(path: str | None = None):
     L.mi_query_launch.restype = i32
     L.mi_device_error.argtypes = [ip, i32]
     L.mi_device_error.restype = i32
+    L.mi_set_wait_test.argtypes = [i64, i32]
+    L.mi_set_wait_test.restype = i32
     L.mi_error_string.argtypes = [i32]
     L.mi_error_string.restype = ctypes.c_char_p
     L.mi_last_cuda_error.argtypes = []
     L.mi_last_cuda_error.restype = ctypes.c_char_p
     L.mi_abi_version.argtypes = []
     L.mi_abi_version.restype = i32
-    L.mi_inverse_descr_f32.argtypes = [vp, vp, vp, vp, vp, vp, i64, ctypes.c_uint32, ctypes.c_uint32, vp,
+    L.mi_inverse_descr_f32.argtypes = [vp, i64, vp, vp, vp, vp, vp, i64, ctypes.c_uint32, ctypes.c_uint32, vp,
                                        ctypes.c_size_t, vp]
     L.mi_inverse_descr_f32.restype = i32
-    L.mi_inverse_descr_noalloc_f32.argtypes = [vp, vp, vp, vp, vp, vp, i64, ctypes.c_uint32, ctypes.c_uint32, vp]
+    L.mi_inverse_descr_noalloc_f32.argtypes = [vp, i64, vp, vp, vp, vp, vp, i64, ctypes.c_uint32, ctypes.c_uint32,
+                                               vp]
     L.mi_inverse_descr_noalloc_f32.restype = i32
     L.mi_newton_schulz_f32.argtypes = [vp, vp, i64, i32, i32, vp]
     L.mi_newton_schulz_f32.restype = i32
@@ -121,4 +124,5 @@ def exported_symbols() -> list[str]:
         "mi_flag_condition_f32",
         "mi_set_launch_config",
         "mi_get_launch_config",
+        "mi_set_wait_test",
     ]

@@ -32,6 +32,16 @@ static std::vector<device_error_reader>& error_readers() {
     static std::vector<device_error_reader> v;
     return v;
 }
+static std::vector<wait_test_setter>& wait_test_setters() {
+    static std::vector<wait_test_setter> v;
+    return v;
+}
+bool register_wait_test_setter(wait_test_setter fn) {
+    std::lock_guard<std::mutex> lock(error_readers_mu());
+    wait_test_setters().push_back(fn);
+    return true;
+}
+
 bool register_device_error_reader(device_error_reader fn) {
     std::lock_guard<std::mutex> lock(error_readers_mu());
     error_readers().push_back(fn);
@@ -258,6 +268,16 @@ int mi_device_error(int* flags, int clear) {
         if (e != cudaSuccess) return mi::cuda_fail(e, "device error word");
     }
     if (flags) *flags = all;
+    return MI_OK;
+}
+
+int mi_set_wait_test(int64_t wait_limit_cycles, int arm_without_copy) {
+    const long long limit = wait_limit_cycles > 0 ? (long long)wait_limit_cycles : mi::kWaitLimit;
+    std::lock_guard<std::mutex> lock(mi::error_readers_mu());
+    for (mi::wait_test_setter set : mi::wait_test_setters()) {
+        const cudaError_t e = set(limit, arm_without_copy != 0 ? 1 : 0);
+        if (e != cudaSuccess) return mi::cuda_fail(e, "wait test hook");
+    }
     return MI_OK;
 }
 

@@ -21,7 +21,14 @@ constexpr size_t kOffList = 4096;                // int32[count]
 // Bucket counts: a shared-memory histogram per block, then one global
 // atomic per non-empty bucket per block (a million descriptors land on a few
 // dozen buckets, so per-descriptor global atomics would serialise).
-__global__ void descr_count(const int32_t* __restrict__ ns, const int32_t* __restrict__ flags, long long count,
+// A descriptor is well-formed when n is 1..32, the flag a pivot mode, and its
+// matrix lies inside the packed buffer of `packed` floats.
+__device__ __forceinline__ bool descr_ok(int n, int f, long long off, long long packed) {
+    return n >= 1 && n <= 32 && f >= 0 && f <= 3 && off >= 0 && off <= packed - (long long)n * n;
+}
+
+__global__ void descr_count(const int32_t* __restrict__ ns, const int32_t* __restrict__ flags,
+                            const long long* __restrict__ offsets, long long packed, long long count,
                             unsigned long long* __restrict__ counts, int32_t* __restrict__ info) {
     __shared__ unsigned int hist[kBuckets];
     for (int b = threadIdx.x; b < kBuckets; b += blockDim.x) hist[b] = 0u;
@@ -29,7 +36,7 @@ __global__ void descr_count(const int32_t* __restrict__ ns, const int32_t* __res
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < count;
          i += (long long)gridDim.x * blockDim.x) {
         const int n = ns[i], f = flags[i];
-        if (n >= 1 && n <= 32 && f >= 0 && f <= 3) atomicAdd(&hist[(n - 1) * 4 + f], 1u);
+        if (descr_ok(n, f, offsets[i], packed)) atomicAdd(&hist[(n - 1) * 4 + f], 1u);
         else if (info != nullptr) info[i] = -1;   // malformed descriptor: reported, not processed
     }
     __syncthreads();
@@ -61,7 +68,8 @@ __global__ void descr_scan(const unsigned long long* __restrict__ counts, unsign
 // descriptor within its bucket in shared memory, reserves the chunk's range
 // of every bucket with one global atomic, then writes the indices.  (Order
 // within a bucket is not significant: each matrix is independent.)
-__global__ void descr_scatter(const int32_t* __restrict__ ns, const int32_t* __restrict__ flags, long long count,
+__global__ void descr_scatter(const int32_t* __restrict__ ns, const int32_t* __restrict__ flags,
+                              const long long* __restrict__ offsets, long long packed, long long count,
                               unsigned long long* __restrict__ cursors, int32_t* __restrict__ list) {
     __shared__ unsigned int hist[kBuckets];
     __shared__ unsigned long long base[kBuckets];
@@ -73,7 +81,7 @@ __global__ void descr_scatter(const int32_t* __restrict__ ns, const int32_t* __r
         unsigned int rank = 0u;
         if (i < count) {
             const int n = ns[i], f = flags[i];
-            if (n >= 1 && n <= 32 && f >= 0 && f <= 3) {
+            if (descr_ok(n, f, offsets[i], packed)) {
                 bucket = (n - 1) * 4 + f;
                 rank = atomicAdd(&hist[bucket], 1u);
             }
@@ -99,10 +107,10 @@ size_t mi_descr_workspace_bytes(int64_t count) {
     return (mi::kOffList + 4 * (size_t)count + 255) & ~(size_t)255;
 }
 
-int mi_inverse_descr_f32(float* d_packed, const int64_t* d_offsets, const int32_t* d_n, const int32_t* d_flags,
-                         int32_t* d_perm, int32_t* d_info, int64_t count, uint32_t n_mask, uint32_t mode_mask,
-                         void* d_workspace, size_t workspace_bytes, void* stream) {
-    if (count < 0 || count > 0x7fffffffLL) return MI_ERR_INVALID_VALUE;
+int mi_inverse_descr_f32(float* d_packed, int64_t packed_floats, const int64_t* d_offsets, const int32_t* d_n,
+                         const int32_t* d_flags, int32_t* d_perm, int32_t* d_info, int64_t count, uint32_t n_mask,
+                         uint32_t mode_mask, void* d_workspace, size_t workspace_bytes, void* stream) {
+    if (count < 0 || count > 0x7fffffffLL || packed_floats < 0) return MI_ERR_INVALID_VALUE;
     if (count == 0) return MI_OK;
     if (d_packed == nullptr || d_offsets == nullptr || d_n == nullptr || d_flags == nullptr || d_workspace == nullptr)
         return MI_ERR_NULL_POINTER;
@@ -123,15 +131,15 @@ int mi_inverse_descr_f32(float* d_packed, const int64_t* d_offsets, const int32_
     const int sms = mi::device_sm_count();
     long long blocks = (count + 255) / 256;
     if (blocks > 4LL * sms) blocks = 4LL * sms;
-    mi::descr_count<<<(unsigned)blocks, 256, 0, st>>>(d_n, d_flags, count, counts, d_info);
+    const long long* off64 = reinterpret_cast<const long long*>(d_offsets);
+    mi::descr_count<<<(unsigned)blocks, 256, 0, st>>>(d_n, d_flags, off64, packed_floats, count, counts, d_info);
     mi::descr_scan<<<1, mi::kBuckets, 0, st>>>(counts, cursors, ranges);
-    mi::descr_scatter<<<(unsigned)blocks, 256, 0, st>>>(d_n, d_flags, count, cursors, list);
+    mi::descr_scatter<<<(unsigned)blocks, 256, 0, st>>>(d_n, d_flags, off64, packed_floats, count, cursors, list);
     e = cudaGetLastError();
     if (e != cudaSuccess) return mi::set_cuda_error(e, "descriptor bucketing");
 
     const mi::ilaunch_fn* tables[4] = {mi::kITableNone, mi::kITableReference, mi::kITableReferenceSerial,
                                        mi::kITablePartial};
-    const long long* off64 = reinterpret_cast<const long long*>(d_offsets);
     for (int n = 1; n <= 32; n++) {
         if (!((n_mask >> (n - 1)) & 1u)) continue;
         for (int mode = 0; mode < 4; mode++) {

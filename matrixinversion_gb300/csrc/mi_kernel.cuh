@@ -110,6 +110,35 @@ cudaError_t read_device_error(int* flags, bool clear) {
 [[maybe_unused]] const bool g_device_error_registered = register_device_error_reader(&read_device_error);
 }  // namespace
 
+// Test hook of the bounded tile-copy waits (per module, like the error word):
+// the longest wait in SM clocks, and a switch under which a warp arms its copy
+// barrier with the expected bytes but issues no copy -- the barrier then never
+// completes, nothing is in flight, and the wait runs out after the limit.
+// Read once per launch by mi_inverse_kernel and mi_wide_kernel; set through
+// mi_set_wait_test.
+__device__ long long g_wait_limit = kWaitLimit;
+__device__ int g_wait_arm_only = 0;
+
+using wait_test_setter = cudaError_t (*)(long long limit, int arm_only);
+bool register_wait_test_setter(wait_test_setter fn);   // mi_api.cu
+
+// Bounded wait on a tile-copy barrier with the limit of the test hook, read
+// only once the barrier is found incomplete (no register held across the
+// kernel's loop).
+__device__ __forceinline__ bool mbar_wait_copy(uint64_t* bar, uint32_t parity) {
+    if (mbar_try_wait(bar, parity)) return true;
+    return mbar_wait(bar, parity, *(volatile long long*)&g_wait_limit);
+}
+
+namespace {
+cudaError_t set_wait_test(long long limit, int arm_only) {
+    cudaError_t e = cudaMemcpyToSymbol(g_wait_limit, &limit, sizeof(limit));
+    if (e == cudaSuccess) e = cudaMemcpyToSymbol(g_wait_arm_only, &arm_only, sizeof(arm_only));
+    return e;
+}
+[[maybe_unused]] const bool g_wait_test_registered = register_wait_test_setter(&set_wait_test);
+}  // namespace
+
 __host__ __device__ constexpr int pow2_at_least(int n) { return n <= 4 ? 4 : (n <= 8 ? 8 : (n <= 16 ? 16 : 32)); }
 
 // Lanes per matrix used by default (n <= 8 runs one thread per matrix):
@@ -1187,11 +1216,15 @@ __global__ void __launch_bounds__(256, 2) mi_inverse_kernel(float* __restrict__ 
                     long long w0, w1;
                     window(g, w0, w1);
                     mbar_arrive_expect_tx(sm.bar, (uint32_t)((w1 - w0) * 4));
-                    bulk_load(sm.slot, A + w0, (uint32_t)((w1 - w0) * 4), sm.bar);
+                    if (g_wait_arm_only == 0) bulk_load(sm.slot, A + w0, (uint32_t)((w1 - w0) * 4), sm.bar);
                 } else {
                     mbar_arrive_expect_tx(sm.bar, (uint32_t)(K::kSlot * 4));
-                    if (copy_mode == kCopyTensor) tma_load_3d(sm.slot, &tmap, 0, 0, (int)first, sm.bar);
-                    else bulk_load(sm.slot, A + first * NN, (uint32_t)(K::kSlot * 4), sm.bar);
+                    if (g_wait_arm_only != 0) {
+                    } else if (copy_mode == kCopyTensor) {
+                        tma_load_3d(sm.slot, &tmap, 0, 0, (int)first, sm.bar);
+                    } else {
+                        bulk_load(sm.slot, A + first * NN, (uint32_t)(K::kSlot * 4), sm.bar);
+                    }
                 }
             }
         } else {
@@ -1217,7 +1250,7 @@ __global__ void __launch_bounds__(256, 2) mi_inverse_kernel(float* __restrict__ 
         const int shift = (copy_mode == kCopyWindow && async_g) ? (int)((first * NN) & 3) : 0;
         if (async_g) {
             // lanes time their waits separately, so the warp decides together
-            if (!__all_sync(kFull, mbar_wait(sm.bar, phase & 1u, kWaitLimit))) {
+            if (!__all_sync(kFull, mbar_wait_copy(sm.bar, phase & 1u))) {
                 timed_out = true;
                 break;
             }
@@ -1259,7 +1292,7 @@ __global__ void __launch_bounds__(256, 2) mi_inverse_kernel(float* __restrict__ 
         atomicOr(&g_device_error, 1);
         // the copy may still land in this warp's slot: wait for it once more,
         // bounded, before the warp leaves
-        mbar_wait(sm.bar, phase & 1u, kWaitLimit);
+        mbar_wait_copy(sm.bar, phase & 1u);
     }
     if (lane == 0) bulk_wait_all();
 }

@@ -313,7 +313,7 @@ __global__ void __launch_bounds__(WideGeom::kThreadsMax, 1)
     auto issue = [&](long long g) {
         if (lane == 0) {
             mbar_arrive_expect_tx(bar, (uint32_t)(G::kSlot * 4));
-            tma_load_3d(slot, &tmap, 0, 0, (int)(g * G::M), bar);
+            if (g_wait_arm_only == 0) tma_load_3d(slot, &tmap, 0, 0, (int)(g * G::M), bar);
         }
     };
 
@@ -324,7 +324,7 @@ __global__ void __launch_bounds__(WideGeom::kThreadsMax, 1)
     while (g < groups) {
         const long long first = g * G::M;
         // lanes time their waits separately, so the warp decides together
-        if (!__all_sync(kFull, mbar_wait(bar, phase & 1u, kWaitLimit))) {
+        if (!__all_sync(kFull, mbar_wait_copy(bar, phase & 1u))) {
             timed_out = true;
             break;
         }
@@ -349,7 +349,7 @@ __global__ void __launch_bounds__(WideGeom::kThreadsMax, 1)
         atomicOr(&g_device_error, 1);
         // the copy may still land in this warp's slot: wait for it once more,
         // bounded, before the warp leaves
-        mbar_wait(bar, phase & 1u, kWaitLimit);
+        mbar_wait_copy(bar, phase & 1u);
     }
     if (lane == 0) bulk_wait_all();
 }

@@ -94,7 +94,8 @@ def batched_inverse_descr_(packed, offsets, ns, flags, *, perm=None, info=None, 
     st = (stream or torch.cuda.current_stream(dev)).cuda_stream
     with torch.cuda.device(dev):
         status = L.mi_inverse_descr_f32(
-            ctypes.c_void_p(packed.data_ptr()), ctypes.c_void_p(offsets.data_ptr()), ctypes.c_void_p(ns.data_ptr()),
+            ctypes.c_void_p(packed.data_ptr()), packed.numel(), ctypes.c_void_p(offsets.data_ptr()),
+            ctypes.c_void_p(ns.data_ptr()),
             ctypes.c_void_p(flags.data_ptr()), ctypes.c_void_p(perm.data_ptr() if perm is not None else 0),
             ctypes.c_void_p(info.data_ptr() if info is not None else 0), count, n_mask & 0xFFFFFFFF,
             mode_mask & 0xF, ctypes.c_void_p(workspace.data_ptr()), workspace.numel() * workspace.element_size(),

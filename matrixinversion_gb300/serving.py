@@ -221,7 +221,7 @@ class CudaServer:
             elif coalesce:
                 offs = torch.sub(self.d_off[m0:m1], base, out=self.d_rel[m0:m1])
                 status = self.L.mi_inverse_descr_f32(
-                    ctypes.c_void_p(dst.data_ptr()), ctypes.c_void_p(offs.data_ptr()),
+                    ctypes.c_void_p(dst.data_ptr()), dst.numel(), ctypes.c_void_p(offs.data_ptr()),
                     ctypes.c_void_p(self.d_n[m0:m1].data_ptr()), ctypes.c_void_p(self.d_flag[m0:m1].data_ptr()),
                     None, ctypes.c_void_p(self.d_info[m0:m1].data_ptr()), m1 - m0, self.n_mask, 1 << self.pivot,
                     ctypes.c_void_p(self.ws.data_ptr()), self.ws.numel(), st)
@@ -309,7 +309,7 @@ class CudaServer:
                 torch.cuda._sleep(200_000)
                 e0.record()
                 self.check(self.L.mi_inverse_descr_f32(
-                    ctypes.c_void_p(work.data_ptr()), ctypes.c_void_p(self.d_off.data_ptr()),
+                    ctypes.c_void_p(work.data_ptr()), work.numel(), ctypes.c_void_p(self.d_off.data_ptr()),
                     ctypes.c_void_p(self.d_n.data_ptr()), ctypes.c_void_p(self.d_flag.data_ptr()), None,
                     ctypes.c_void_p(self.d_info.data_ptr()), m, self.n_mask, 1 << self.pivot,
                     ctypes.c_void_p(self.ws.data_ptr()), self.ws.numel(), st))

@@ -116,6 +116,30 @@ def ref_inverse_f32(A: np.ndarray, mode: str = "reference"):
     return X, perm, info
 
 
+def lu_growth_bound(A: np.ndarray, perm: np.ndarray, X64: np.ndarray | None = None) -> np.ndarray:
+    """|| |L| |U| |X| ||_inf per matrix, with P A = L U factored in FP64 in the
+    given pivot order (perm[b][k] = input row placed at step k, no further
+    pivoting) and X the FP64 inverse.  n u times this is the componentwise
+    residual bound of an LU-based inverse that used that pivot sequence: it
+    grows with the sequence's own element growth, so it measures a kernel
+    against what its pivot rule allows rather than against one rounding order.
+    """
+    A = np.asarray(A, dtype=np.float64)
+    b, n, _ = A.shape
+    Uf = np.take_along_axis(A, np.asarray(perm, dtype=np.int64)[:, :, None], axis=1).copy()
+    L = np.zeros_like(Uf)
+    with np.errstate(divide="ignore", invalid="ignore", over="ignore"):
+        for k in range(n):
+            L[:, k, k] = 1.0
+            m = Uf[:, k + 1:, k] / Uf[:, k:k + 1, k]
+            L[:, k + 1:, k] = m
+            Uf[:, k + 1:, :] -= m[:, :, None] * Uf[:, k:k + 1, :]
+            Uf[:, k + 1:, k] = 0.0
+        if X64 is None:
+            X64 = np.linalg.inv(A)
+        return (np.abs(L) @ np.abs(Uf) @ np.abs(X64)).sum(2).max(1)
+
+
 def residual(A: np.ndarray, X: np.ndarray) -> np.ndarray:
     """Per matrix [||AX - I||_inf, max|AX - I|] in FP64."""
     A = np.ascontiguousarray(A, dtype=np.float32)

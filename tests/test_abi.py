@@ -85,7 +85,7 @@ def test_c_caller_links_and_runs_without_gpu(lib, tmp_path):
 def test_query_and_errors_without_gpu(lib):
     from matrixinversion_gb300 import _lib
 
-    assert lib.mi_abi_version() == 1
+    assert lib.mi_abi_version() == 2
     lanes, mpw, smem, tpb = (ctypes.c_int() for _ in range(4))
     # n <= 15: one thread per matrix, staged through shared memory except at
     # n = 2, where each thread moves its matrix with 16-byte copies; larger n:
@@ -173,20 +173,23 @@ def test_noalloc_and_descriptor_argument_checks_without_gpu(lib):
     from matrixinversion_gb300 import _lib
 
     d = lib.mi_inverse_descr_f32
-    assert d(None, None, None, None, None, None, 0, 0, 0, None, 0, None) == _lib.MI_OK
-    assert d(None, None, None, None, None, None, -1, 0, 0, None, 0, None) == _lib.MI_ERR_INVALID_VALUE
-    assert d(None, None, None, None, None, None, 4, 0, 0, None, 0, None) == _lib.MI_ERR_NULL_POINTER
+    big = 1 << 30
+    assert d(None, 0, None, None, None, None, None, 0, 0, 0, None, 0, None) == _lib.MI_OK
+    assert d(None, 0, None, None, None, None, None, -1, 0, 0, None, 0, None) == _lib.MI_ERR_INVALID_VALUE
+    assert d(None, -1, None, None, None, None, None, 4, 0, 0, None, 0, None) == _lib.MI_ERR_INVALID_VALUE
+    assert d(None, big, None, None, None, None, None, 4, 0, 0, None, 0, None) == _lib.MI_ERR_NULL_POINTER
     p = ctypes.c_void_p(0x100000)
-    assert d(ctypes.c_void_p(0x100002), p, p, p, None, None, 4, 0, 0, p, 1 << 20, None) == _lib.MI_ERR_MISALIGNED
-    assert d(p, p, p, p, None, None, 4, 0, 0, ctypes.c_void_p(0x100010), 1 << 20, None) == _lib.MI_ERR_MISALIGNED
+    assert d(ctypes.c_void_p(0x100002), big, p, p, p, None, None, 4, 0, 0, p, 1 << 20, None) == _lib.MI_ERR_MISALIGNED
+    assert d(p, big, p, p, p, None, None, 4, 0, 0, ctypes.c_void_p(0x100010), 1 << 20, None) == _lib.MI_ERR_MISALIGNED
     need = lib.mi_descr_workspace_bytes(4)
-    assert d(p, p, p, p, None, None, 4, 0, 0, p, need - 1, None) == _lib.MI_ERR_INVALID_VALUE
+    assert d(p, big, p, p, p, None, None, 4, 0, 0, p, need - 1, None) == _lib.MI_ERR_INVALID_VALUE
     for count in (0, 1, 1000, 262144):
         assert lib.mi_descr_workspace_bytes(count) == (4096 + 4 * count + 255) // 256 * 256
     na = lib.mi_inverse_descr_noalloc_f32
-    assert na(None, None, None, None, None, None, 0, 0, 0, None) == _lib.MI_OK
-    assert na(None, None, None, None, None, None, -5, 0, 0, None) == _lib.MI_ERR_INVALID_VALUE
-    assert na(p, p, p, p, None, None, _lib.MI_NOALLOC_MAX_COUNT + 1, 0, 0, None) == _lib.MI_ERR_SCRATCH_LIMIT
+    assert na(None, 0, None, None, None, None, None, 0, 0, 0, None) == _lib.MI_OK
+    assert na(None, 0, None, None, None, None, None, -5, 0, 0, None) == _lib.MI_ERR_INVALID_VALUE
+    assert na(p, -1, p, p, p, None, None, 4, 0, 0, None) == _lib.MI_ERR_INVALID_VALUE
+    assert na(p, big, p, p, p, None, None, _lib.MI_NOALLOC_MAX_COUNT + 1, 0, 0, None) == _lib.MI_ERR_SCRATCH_LIMIT
     # refinement entry points
     assert lib.mi_newton_schulz_f32(None, None, 4, 16, 1, None) == _lib.MI_ERR_INVALID_VALUE
     assert lib.mi_newton_schulz_f32(None, None, 4, 32, 5, None) == _lib.MI_ERR_INVALID_VALUE

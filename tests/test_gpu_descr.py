@@ -77,15 +77,21 @@ def test_malformed_descriptors_and_masks(mi_gpu, oracle):
     bad_n[5] = 33
     bad_f = flags.copy()
     bad_f[7] = 9
+    # matrices outside the packed buffer: a negative offset, and one that ends
+    # a float past the end
+    bad_off = offsets.copy()
+    bad_off[9] = -4
+    bad_off[11] = packed.size - int(ns_[11]) ** 2 + 1
     d_packed = torch.from_numpy(packed).cuda()
     info = torch.zeros(len(mats), dtype=torch.int32, device="cuda")
-    descr.batched_inverse_descr_(d_packed, torch.from_numpy(offsets).cuda(), torch.from_numpy(bad_n).cuda(),
+    descr.batched_inverse_descr_(d_packed, torch.from_numpy(bad_off).cuda(), torch.from_numpy(bad_n).cuda(),
                                  torch.from_numpy(bad_f).cuda(), info=info)
     info = info.cpu().numpy()
-    got = descr.unpack(d_packed.cpu().numpy(), offsets, ns_)
-    for i in (3, 5, 7):
-        assert info[i] == -1
-        assert np.array_equal(got[i], mats[i])        # untouched
+    out = d_packed.cpu().numpy()
+    got = descr.unpack(out, offsets, ns_)
+    for i in (3, 5, 7, 9, 11):
+        assert info[i] == -1, i
+        assert np.array_equal(got[i], mats[i]), i     # untouched
     want, _, _ = contiguous_results(mi_gpu, mats, flags)
     assert np.array_equal(got[0], want[0])
     # masks that exclude a present size leave those matrices untouched

@@ -6,15 +6,19 @@ Tolerances, stated once:
     produced (tests/golden).  The rules compare raw inputs only, so no
     floating-point slack is involved.
   * inverse, pivoted modes: per matrix
-        ||AX - I||_inf <= 32 * r_port + 8 n u || |A| |X64| ||_inf,
-    where r_port is the residual of the reference algorithm itself (FP32
-    Doolittle + comp_inv, oracle port) with the same pivots, X64 the FP64
-    oracle inverse and u = 2^-24 (the second term is the componentwise
-    residual bound of a stable inversion, the first the reference rule's own
-    instability); and the batch median of ||AX - I||_inf within 2x of the
-    port's median.  (The reference's pivot rule is not stable; two FP32
-    evaluation orders of the same pivot sequence differ by up to ~10x on
-    single matrices.)
+        ||AX - I||_inf <= max(8 n u || |L| |U| |X64| ||_inf, 2 r_port),
+    where L U = P A is factored in FP64 in the kernel's own pivot order (the
+    oracle's lu_growth_bound), X64 is the FP64 inverse and u = 2^-24 -- the
+    componentwise residual bound of an LU-based inverse with that pivot
+    sequence, which grows with the sequence's element growth (the reference
+    rule is not stable) -- or, where even the reference algorithm breaks that
+    bound (element growth so large that FP32 factors part from FP64 ones:
+    about one matrix in 10^5), within 2x of r_port, the residual of the
+    reference algorithm itself (FP32 Doolittle + comp_inv, the oracle's port)
+    with the same pivots; and the batch median of ||AX - I||_inf within 2x of
+    the port's median.  Over 1,000,000-matrix batches, two FP32 evaluation
+    orders of one unstable pivot sequence differ by up to ~400x on single
+    matrices, so no fixed multiple of r_port alone bounds them.
   * inverse, no pivoting (diagonally dominant inputs): ||AX - I||_inf <= 1e-5
     and max |X - X64| <= 1e-5 * max |X64| per matrix against the FP64 oracle.
 """
@@ -34,14 +38,13 @@ def gpu_inverse(mi, A, mode, **kw):
     return X.cpu().numpy(), perm.cpu().numpy(), info.cpu().numpy()
 
 
-def residual_bound(oracle, A, mode):
+def residual_bound(oracle, A, mode, perm=None):
     """Per-matrix tolerance on ||AX - I||_inf and the port's residuals."""
     n = A.shape[-1]
-    Xp, _, _ = oracle.ref_inverse_f32(A, mode)
+    Xp, pp, _ = oracle.ref_inverse_f32(A, mode)
     rp = oracle.residual(A, Xp)[:, 0]
-    X64, _, _ = oracle.inverse_f64(A, "partial")
-    comp = np.einsum("bij,bjk->bik", np.abs(A.astype(np.float64)), np.abs(X64)).sum(2).max(1)
-    return 32.0 * rp + 8.0 * n * U * comp, rp
+    growth = oracle.lu_growth_bound(A, pp if perm is None else perm)
+    return np.maximum(8.0 * n * U * growth, 2.0 * rp), rp
 
 
 def check_pivoted_accuracy(oracle, A, X, mode):

@@ -56,11 +56,12 @@ def test_noalloc_matches_workspace_entry_point_twice(mi_gpu, oracle):
         info_a = torch.full((count,), -9, dtype=torch.int32, device="cuda")
         info_b = info_a.clone()
         ws = torch.empty(descr.workspace_bytes(count), dtype=torch.uint8, device="cuda")
-        st = L.mi_inverse_descr_f32(_ptr(a), _ptr(d_off), _ptr(d_n), _ptr(d_f), _ptr(perm_a), _ptr(info_a), count, 0,
-                                    0, _ptr(ws), ws.numel(), ctypes.c_void_p(stream.cuda_stream))
+        st = L.mi_inverse_descr_f32(_ptr(a), a.numel(), _ptr(d_off), _ptr(d_n), _ptr(d_f), _ptr(perm_a),
+                                    _ptr(info_a), count, 0, 0, _ptr(ws), ws.numel(),
+                                    ctypes.c_void_p(stream.cuda_stream))
         assert st == 0, _lib.load().mi_error_string(st)
-        st = L.mi_inverse_descr_noalloc_f32(_ptr(b), _ptr(d_off), _ptr(d_n), _ptr(d_f), _ptr(perm_b), _ptr(info_b),
-                                            count, 0, 0, ctypes.c_void_p(stream.cuda_stream))
+        st = L.mi_inverse_descr_noalloc_f32(_ptr(b), b.numel(), _ptr(d_off), _ptr(d_n), _ptr(d_f), _ptr(perm_b),
+                                            _ptr(info_b), count, 0, 0, ctypes.c_void_p(stream.cuda_stream))
         assert st == 0, (st, L.mi_error_string(st), L.mi_last_cuda_error())
         torch.cuda.synchronize()
         a, b = a.cpu().numpy(), b.cpu().numpy()
@@ -83,7 +84,7 @@ def test_noalloc_rejects_count_above_limit(mi_gpu):
     x = torch.zeros(16, dtype=torch.float32, device="cuda")
     o = torch.zeros(1, dtype=torch.int64, device="cuda")
     i = torch.ones(1, dtype=torch.int32, device="cuda")
-    st = L.mi_inverse_descr_noalloc_f32(_ptr(x), _ptr(o), _ptr(i), _ptr(i), None, None,
+    st = L.mi_inverse_descr_noalloc_f32(_ptr(x), x.numel(), _ptr(o), _ptr(i), _ptr(i), None, None,
                                         _lib.MI_NOALLOC_MAX_COUNT + 1, 0, 0, None)
     assert st == _lib.MI_ERR_SCRATCH_LIMIT
     assert b"MI_NOALLOC_MAX_COUNT" in L.mi_error_string(st)
