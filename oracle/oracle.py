@@ -29,9 +29,12 @@ _i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
 _i64 = ctypes.c_int64
 
 
-def build(quiet: bool = True) -> None:
-    """Compile the oracle library (and the reference emulation where possible)."""
-    out = subprocess.run(["make", "-C", HERE, "all"], capture_output=True, text=True)
+def build(quiet: bool = True, ref_root: str | None = None) -> None:
+    """Compile the oracle library, and the reference emulation when the
+    reference project's root is given (ref_root, else the MI_REF_ROOT
+    environment variable) and holds its sources."""
+    ref_root = ref_root or os.environ.get("MI_REF_ROOT", "")
+    out = subprocess.run(["make", "-C", HERE, "all", f"REF_ROOT={ref_root}"], capture_output=True, text=True)
     if out.returncode != 0:
         raise RuntimeError("oracle build failed:\n" + out.stdout + out.stderr)
     if not quiet:

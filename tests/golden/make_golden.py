@@ -5,7 +5,7 @@ unchanged against the host-thread CUDA stand-in in oracle/ref_emu and built
 by oracle/Makefile).  The committed .npz is what the tests read; this script
 only regenerates it:
 
-    python tests/golden/make_golden.py [REF_ROOT]
+    python tests/golden/make_golden.py REF_ROOT      (or MI_REF_ROOT=... in the environment)
 
 Contents, for every n in 1..32:
   uniform inputs   : MT19937(seed) uniform [-1, 1) batches (regenerated by the
@@ -49,7 +49,10 @@ def tie_matrices(rng: np.random.RandomState, count: int, n: int) -> np.ndarray:
     return rng.randint(-3, 4, size=(count, n, n)).astype(np.int8)
 
 
-def main(ref_root: str = "/root/reference") -> None:
+def main(ref_root: str | None = None) -> None:
+    ref_root = ref_root or os.environ.get("MI_REF_ROOT")
+    if not ref_root:
+        raise SystemExit("usage: make_golden.py REF_ROOT (or set MI_REF_ROOT): the reference project's root")
     subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "all", f"REF_ROOT={ref_root}"], check=True)
     if not O.ref_available():
         raise SystemExit("reference emulation was not built")
