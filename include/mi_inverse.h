@@ -272,6 +272,38 @@ int mi_get_launch_config(int n, int pivot, int* threads_per_block);
 const char* mi_error_string(int status);
 /* Text of the last CUDA error seen by this thread ("" if none). */
 const char* mi_last_cuda_error(void);
+/*
+ * Serving loop (no counterpart in the reference, which inverts one pre-loaded
+ * batch per process).  Serves num_requests requests -- request r: k[r]
+ * matrices of size n[r] (1..32), pivot mode `pivot`, arriving arrival_s[r]
+ * seconds after the call starts (non-decreasing) -- and returns when all have
+ * completed, with latency_s[r] = completion - arrival.  Runs on the calling
+ * thread; every launch and copy is issued from native code.
+ *   Copies (d_ring == NULL): request r's matrices are read from the pinned
+ *     host ring h_in + ring_off[r] (floats) and written back to h_out at the
+ *     same offset.  d_pool: the device pool of pool_floats floats, carved by
+ *     the caller once (the HBM budget); an arrived request is admitted, first
+ *     come first served, as soon as a free extent of the pool holds it, and
+ *     its extent is freed when its own results have reached h_out.  A request
+ *     larger than the pool returns MI_ERR_SCRATCH_LIMIT.
+ *   Resident (d_ring != NULL): the matrices already sit in device memory at
+ *     d_ring + ring_off[r] and are inverted in place (no copies, d_pool and the
+ *     host rings unused); a request completes with its batch's kernels.
+ *   Batching: while fewer than two batches compute, every admitted request
+ *     not yet computed (coalesce != 0; at most max_batch_matrices matrices)
+ *     or the next one (coalesce == 0) goes out as one launch.
+ *   d_scratch: device scratch of mi_serve_scratch_bytes(max_batch_matrices)
+ *     bytes, 256-byte aligned.  The call makes its own streams, events and a
+ *     pinned staging buffer for the descriptor tables at its start and frees
+ *     them before it returns.
+ *   stats (nullable) int64[2]: batches launched, peak pool floats in use.
+ */
+size_t mi_serve_scratch_bytes(int64_t max_batch_matrices);
+int mi_serve_run(int64_t num_requests, const double* arrival_s, const int64_t* k, const int32_t* n,
+                 const int64_t* ring_off, const float* h_in, float* h_out, float* d_ring, float* d_pool,
+                 int64_t pool_floats, void* d_scratch, size_t scratch_bytes, int64_t max_batch_matrices, int pivot,
+                 int coalesce, double* latency_s, double* wall_s, int64_t* stats);
+
 /* MI_ABI_VERSION of the loaded library, to check against the header a
    caller was built with (no counterpart in the reference, which has no
    library). */

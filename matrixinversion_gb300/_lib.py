@@ -64,6 +64,11 @@ def load(path: str | None = None):
     L.mi_device_error.restype = i32
     L.mi_set_wait_test.argtypes = [i64, i32]
     L.mi_set_wait_test.restype = i32
+    L.mi_serve_scratch_bytes.argtypes = [i64]
+    L.mi_serve_scratch_bytes.restype = ctypes.c_size_t
+    L.mi_serve_run.argtypes = [i64, vp, vp, vp, vp, vp, vp, vp, vp, i64, vp, ctypes.c_size_t, i64, i32, i32, vp, vp,
+                               vp]
+    L.mi_serve_run.restype = i32
     L.mi_error_string.argtypes = [i32]
     L.mi_error_string.restype = ctypes.c_char_p
     L.mi_last_cuda_error.argtypes = []
@@ -125,4 +130,6 @@ def exported_symbols() -> list[str]:
         "mi_set_launch_config",
         "mi_get_launch_config",
         "mi_set_wait_test",
+        "mi_serve_scratch_bytes",
+        "mi_serve_run",
     ]

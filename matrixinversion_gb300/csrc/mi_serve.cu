@@ -1,0 +1,261 @@
+// mi_serve.cu -- the serving loop in native code (host side of the C ABI's
+// mi_serve_run).  No counterpart in the reference, which inverts one
+// pre-loaded batch per process.
+//
+// Requests (k matrices of one size n each) arrive at given times.  The loop
+// runs on the calling thread without returning to the caller until every
+// request has completed:
+//
+//   * admission: first come, first served; an arrived request is admitted
+//     when the device pool (the HBM budget, carved once by the caller) has a
+//     free extent for it (ExtentPool, first fit), and its host-to-device copy
+//     goes out at once on the copy stream;
+//   * batching: whenever fewer than two batches are computing, every admitted
+//     request not yet computed goes into one launch -- one descriptor call
+//     over the pool (its matrices' offsets into the pool staged through a
+//     pinned table), or one contiguous call for a batch of a single request;
+//   * completion, per request: its results are copied back to its place in
+//     the host ring on the copy-out stream with an event of its own; when the
+//     loop sees that event it records the request's completion time and frees
+//     its extent, so a request's latency does not wait for the rest of its
+//     batch to leave and its memory serves the next arrivals at once.
+//
+// With requests already in device memory (d_ring != NULL: an upstream device
+// stage wrote them there; the caller counts that memory against its budget)
+// there are no copies: batches are inverted in place and a request completes
+// with its batch's kernels.
+#include <cuda_runtime.h>
+
+#include <chrono>
+#include <cstdint>
+#include <cstring>
+#include <deque>
+#include <thread>
+#include <vector>
+
+#include "mi_extents.h"
+#include "mi_inverse.h"
+
+namespace mi {
+int set_cuda_error(cudaError_t e, const char* what);   // mi_api.cu
+}
+
+namespace {
+
+constexpr int kInFlight = 2;   // batches computing at once (each owns one descriptor table)
+
+size_t table_bytes(int64_t max_batch) { return ((size_t)max_batch * 16 + 255) & ~(size_t)255; }
+
+// Streams, events and pinned staging of one run, released on every exit.
+struct Resources {
+    cudaStream_t h2d = nullptr, cmp = nullptr, d2h = nullptr;
+    std::vector<cudaEvent_t> events;        // all events made, destroyed at the end
+    std::vector<cudaEvent_t> spare;         // events free for reuse
+    void* staging = nullptr;                // pinned: kInFlight descriptor tables
+    ~Resources() {
+        for (cudaStream_t s : {h2d, cmp, d2h})
+            if (s != nullptr) cudaStreamSynchronize(s);
+        for (cudaEvent_t e : events) cudaEventDestroy(e);
+        for (cudaStream_t s : {h2d, cmp, d2h})
+            if (s != nullptr) cudaStreamDestroy(s);
+        if (staging != nullptr) cudaFreeHost(staging);
+    }
+    cudaError_t event(cudaEvent_t* out) {
+        if (!spare.empty()) {
+            *out = spare.back();
+            spare.pop_back();
+            return cudaSuccess;
+        }
+        cudaError_t e = cudaEventCreateWithFlags(out, cudaEventDisableTiming);
+        if (e == cudaSuccess) events.push_back(*out);
+        return e;
+    }
+};
+
+struct Batch {
+    int64_t first, last;    // requests [first, last), in arrival order
+    cudaEvent_t done;       // the batch's kernels finished
+};
+
+}  // namespace
+
+extern "C" {
+
+size_t mi_serve_scratch_bytes(int64_t max_batch_matrices) {
+    if (max_batch_matrices <= 0) return 0;
+    return kInFlight * table_bytes(max_batch_matrices) + mi_descr_workspace_bytes(max_batch_matrices);
+}
+
+int mi_serve_run(int64_t num_requests, const double* arrival_s, const int64_t* k, const int32_t* n,
+                 const int64_t* ring_off, const float* h_in, float* h_out, float* d_ring, float* d_pool,
+                 int64_t pool_floats, void* d_scratch, size_t scratch_bytes, int64_t max_batch_matrices, int pivot,
+                 int coalesce, double* latency_s, double* wall_s, int64_t* stats) {
+    if (num_requests < 0 || max_batch_matrices <= 0 || pivot < MI_PIVOT_NONE || pivot > MI_PIVOT_PARTIAL)
+        return MI_ERR_INVALID_VALUE;
+    if (num_requests == 0) return MI_OK;
+    const bool resident = d_ring != nullptr;
+    if (arrival_s == nullptr || k == nullptr || n == nullptr || ring_off == nullptr || latency_s == nullptr ||
+        d_scratch == nullptr || (!resident && (h_in == nullptr || h_out == nullptr || d_pool == nullptr)))
+        return MI_ERR_NULL_POINTER;
+    if (scratch_bytes < mi_serve_scratch_bytes(max_batch_matrices) ||
+        (reinterpret_cast<uintptr_t>(d_scratch) & 255u) != 0)
+        return MI_ERR_INVALID_VALUE;
+    // every request must be well-formed, fit one batch, and (with copies) fit the pool
+    std::vector<int64_t> len(num_requests);
+    for (int64_t r = 0; r < num_requests; r++) {
+        if (n[r] < 1 || n[r] > 32 || k[r] < 1 || k[r] > max_batch_matrices || ring_off[r] < 0 ||
+            (r > 0 && arrival_s[r] < arrival_s[r - 1]))
+            return MI_ERR_INVALID_VALUE;
+        len[r] = (k[r] * n[r] * n[r] + 3) / 4 * 4;          // 16-byte aligned extents
+        if (!resident && len[r] > pool_floats) return MI_ERR_SCRATCH_LIMIT;
+    }
+
+    Resources res;
+    cudaError_t e = cudaStreamCreateWithFlags(&res.h2d, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&res.cmp, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&res.d2h, cudaStreamNonBlocking);
+    const size_t tb = table_bytes(max_batch_matrices);
+    if (e == cudaSuccess) e = cudaHostAlloc(&res.staging, kInFlight * tb, cudaHostAllocDefault);
+    if (e != cudaSuccess) return mi::set_cuda_error(e, "serving set-up");
+    unsigned char* scratch = static_cast<unsigned char*>(d_scratch);
+    void* workspace = scratch + kInFlight * tb;
+    const size_t ws_bytes = scratch_bytes - kInFlight * tb;
+    float* base = resident ? d_ring : d_pool;
+    const int64_t base_floats = resident ? INT64_MAX / 2 : pool_floats;
+
+    mi::ExtentPool pool(resident ? 0 : pool_floats);
+    std::vector<int64_t> ext(num_requests, -1);            // pool extent of each admitted request
+    std::vector<double> done(num_requests, -1.0);
+    std::deque<Batch> computing;
+    std::deque<std::pair<int64_t, cudaEvent_t>> leaving;    // results on their way to the host ring
+    int64_t admitted = 0, launched = 0, completed = 0, batches = 0, tables_used = 0;
+
+    const auto t0 = std::chrono::steady_clock::now();
+    auto now = [&] { return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count(); };
+
+    auto fail = [&](cudaError_t err, const char* what) { return mi::set_cuda_error(err, what); };
+
+    while (completed < num_requests) {
+        const double t = now();
+        bool idle = true;
+        // ---- completions: results home (per request), batches finished
+        while (!leaving.empty()) {
+            const cudaError_t q = cudaEventQuery(leaving.front().second);
+            if (q == cudaErrorNotReady) break;
+            if (q != cudaSuccess) return fail(q, "serving: result copy");
+            const int64_t r = leaving.front().first;
+            done[r] = t;
+            pool.release(ext[r], len[r]);
+            res.spare.push_back(leaving.front().second);
+            leaving.pop_front();
+            completed++;
+            idle = false;
+        }
+        while (!computing.empty()) {
+            const cudaError_t q = cudaEventQuery(computing.front().done);
+            if (q == cudaErrorNotReady) break;
+            if (q != cudaSuccess) return fail(q, "serving: batch");
+            if (resident) {
+                for (int64_t r = computing.front().first; r < computing.front().last; r++) done[r] = t;
+                completed += computing.front().last - computing.front().first;
+            }
+            res.spare.push_back(computing.front().done);
+            computing.pop_front();
+            idle = false;
+        }
+        // ---- admission: arrived requests, first come first served, as extents free
+        while (admitted < num_requests && arrival_s[admitted] <= t) {
+            if (!resident) {
+                const int64_t off = pool.alloc(len[admitted]);
+                if (off < 0) break;                          // wait for memory, keep the order
+                ext[admitted] = off;
+                e = cudaMemcpyAsync(d_pool + off, h_in + ring_off[admitted],
+                                    (size_t)(k[admitted] * n[admitted] * n[admitted]) * sizeof(float),
+                                    cudaMemcpyHostToDevice, res.h2d);
+                if (e != cudaSuccess) return fail(e, "serving: request copy");
+            } else {
+                ext[admitted] = ring_off[admitted];
+            }
+            admitted++;
+            idle = false;
+        }
+        // ---- batching: every admitted request not yet computed, into one launch
+        if (launched < admitted && (int)computing.size() < kInFlight) {
+            int64_t last = launched, mats = 0;
+            uint32_t n_mask = 0;
+            while (last < admitted && mats + k[last] <= max_batch_matrices && (coalesce || last == launched)) {
+                mats += k[last];
+                n_mask |= 1u << (n[last] - 1);
+                last++;
+            }
+            cudaEvent_t ready = nullptr;
+            if (!resident) {
+                if ((e = res.event(&ready)) != cudaSuccess || (e = cudaEventRecord(ready, res.h2d)) != cudaSuccess ||
+                    (e = cudaStreamWaitEvent(res.cmp, ready, 0)) != cudaSuccess)
+                    return fail(e, "serving: batch inputs");
+                res.spare.push_back(ready);   // recorded and waited on: free for reuse in stream order
+            }
+            int status = MI_OK;
+            if (last - launched == 1) {
+                status = mi_inverse_f32(base + ext[launched], nullptr, nullptr, k[launched], n[launched], pivot, res.cmp);
+            } else {
+                const int buf = (int)(tables_used++ % kInFlight);   // free: its batch finished (at most 2 in flight)
+                // the table of this batch's mats matrices, packed: offsets, sizes, flags
+                unsigned char* hs = static_cast<unsigned char*>(res.staging) + buf * tb;
+                int64_t* hoff = reinterpret_cast<int64_t*>(hs);
+                int32_t* hn = reinterpret_cast<int32_t*>(hs + 8 * (size_t)mats);
+                int32_t* hf = reinterpret_cast<int32_t*>(hs + 12 * (size_t)mats);
+                int64_t m = 0;
+                for (int64_t r = launched; r < last; r++) {
+                    const int64_t nn = (int64_t)n[r] * n[r];
+                    for (int64_t i = 0; i < k[r]; i++, m++) {
+                        hoff[m] = ext[r] + i * nn;
+                        hn[m] = n[r];
+                        hf[m] = pivot;
+                    }
+                }
+                unsigned char* ds = scratch + buf * tb;
+                e = cudaMemcpyAsync(ds, hs, 16 * (size_t)m, cudaMemcpyHostToDevice, res.cmp);
+                if (e != cudaSuccess) return fail(e, "serving: descriptor table");
+                status = mi_inverse_descr_f32(base, base_floats, reinterpret_cast<int64_t*>(ds),
+                                              reinterpret_cast<int32_t*>(ds + 8 * (size_t)m),
+                                              reinterpret_cast<int32_t*>(ds + 12 * (size_t)m), nullptr, nullptr, m,
+                                              n_mask, 1u << pivot, workspace, ws_bytes, res.cmp);
+            }
+            if (status != MI_OK) return status;
+            Batch b{launched, last, nullptr};
+            if ((e = res.event(&b.done)) != cudaSuccess || (e = cudaEventRecord(b.done, res.cmp)) != cudaSuccess)
+                return fail(e, "serving: batch event");
+            if (!resident) {
+                if ((e = cudaStreamWaitEvent(res.d2h, b.done, 0)) != cudaSuccess) return fail(e, "serving: results");
+                for (int64_t r = launched; r < last; r++) {
+                    cudaEvent_t home = nullptr;
+                    if ((e = cudaMemcpyAsync(h_out + ring_off[r], d_pool + ext[r],
+                                             (size_t)(k[r] * n[r] * n[r]) * sizeof(float), cudaMemcpyDeviceToHost,
+                                             res.d2h)) != cudaSuccess ||
+                        (e = res.event(&home)) != cudaSuccess || (e = cudaEventRecord(home, res.d2h)) != cudaSuccess)
+                        return fail(e, "serving: result copy");
+                    leaving.emplace_back(r, home);
+                }
+            }
+            computing.push_back(b);
+            launched = last;
+            batches++;
+            idle = false;
+        }
+        if (idle) std::this_thread::yield();
+    }
+    double wall = 0.0;
+    for (int64_t r = 0; r < num_requests; r++) {
+        latency_s[r] = done[r] - arrival_s[r];
+        wall = done[r] > wall ? done[r] : wall;
+    }
+    if (wall_s != nullptr) *wall_s = wall;
+    if (stats != nullptr) {
+        stats[0] = batches;
+        stats[1] = pool.peak();
+    }
+    return MI_OK;
+}
+
+}  // extern "C"

@@ -2,27 +2,30 @@
 
 A request holds k matrices of one size n (partial pivoting by default).
 Requests arrive (Poisson, in real time) into a pinned host ring in arrival
-order -- the way a network receive buffer fills -- and the server admits
-them first come, first served into a device pool with a fixed HBM budget:
+order -- the way a network receive buffer fills.  The loop itself is native
+code (`mi_serve_run` in the C ABI, csrc/mi_serve.cu); this module builds the
+trace and the buffers and reads the results:
 
-* the pool is two arena halves carved once at start-up (no allocation on the
-  serving path); a batch takes every arrived request that fits in a free
-  half, so a half is the largest batch and the budget bounds what is resident;
-* one batch = one host-to-device copy of its contiguous span of the ring, one
-  descriptor call (GPU bucketing by size, one persistent launch per size
-  present; a batch of one size stored back to back takes a single contiguous
-  launch instead) and one device-to-host copy into the output ring, on
-  separate copy and compute streams so that consecutive batches overlap;
-* a request completes when the host sees its batch's last copy finish.
+* the device pool is the HBM budget, carved once at start-up (no allocation
+  on the serving path); an arrived request is admitted, first come first
+  served, as soon as a free extent of the pool holds it (first fit, extents
+  merged on release), and its host-to-device copy goes out at once;
+* while fewer than two batches compute, every admitted request not yet
+  computed goes into one launch: one descriptor call over the pool (GPU
+  bucketing by size, one persistent launch per size present), or one
+  contiguous call for a batch of a single request;
+* each request's results return to the output ring with an event of its own;
+  when the loop sees it, the request has completed and its extent is free.
 
 With `resident=True` the requests' matrices already sit in HBM (produced by
-an upstream device stage): batches are inverted in place in the device ring,
-with no copies, and `offline()` gives the plain batched kernel's rate on the
+an upstream device stage, in a device ring that counts against the budget):
+batches are inverted in place, with no copies, a request completes with its
+batch's kernels, and `offline()` gives the plain batched kernel's rate on the
 same matrices for comparison.
 
-The baseline ("per_request") runs the same loop with one request per batch
-and a plain contiguous launch per request.  Both paths run the same kernels
-on the same data, so results are equal bit for bit (tested).
+The baseline ("per_request") runs the same loop with one request per launch.
+Both paths run the same kernels on the same data, so results are equal bit
+for bit (tested).
 
     python -m matrixinversion_gb300.serving --rates 2000,8000,32000 --requests 2000
 """
@@ -44,7 +47,7 @@ PIVOT_PARTIAL = 3
 
 def nvtx_ranges():
     """(push, pop) of NVTX host ranges, so a timeline profiler shows each
-    batch's admission and issue; no-ops where torch was built without NVTX."""
+    serving run; no-ops where torch was built without NVTX."""
     try:
         import torch.cuda.nvtx as nv
 
@@ -97,44 +100,13 @@ def retime(trace: Trace, rate: float, seed: int = 0) -> Trace:
     return Trace(arrival=np.cumsum(gaps) - gaps[0], k=trace.k, n=trace.n, offset=trace.offset)
 
 
-class Batcher:
-    """First come, first served admission under a per-batch float budget.
-
-    next_batch(i, now) returns the end j of the batch [i, j): every request
-    that has arrived by `now`, in order, while the span of the ring it covers
-    fits in `half_floats` (the first request always fits: it is rejected at
-    start-up if it alone exceeds the budget), at most `max_requests` of them.
-    """
-
-    def __init__(self, trace: Trace, half_floats: int, max_requests: int | None = None):
-        self.t = trace
-        self.half = int(half_floats)
-        self.max_requests = max_requests
-        ends = trace.offset + trace.floats
-        if len(trace.k) and int((trace.floats).max()) > self.half:
-            raise ValueError("a request is larger than one pool half; raise the HBM budget")
-        self.ends = ends
-
-    def next_batch(self, i: int, now: float) -> int:
-        t = self.t
-        nreq = len(t.k)
-        if i >= nreq or t.arrival[i] > now:
-            return i
-        arrived = int(np.searchsorted(t.arrival, now, side="right"))
-        limit = t.offset[i] + self.half
-        fit = int(np.searchsorted(self.ends, limit, side="right"))
-        j = min(arrived, fit)
-        if self.max_requests is not None:
-            j = min(j, i + self.max_requests)
-        return max(j, i + 1)
-
-
 class CudaServer:
-    """The device side: pinned rings, the two arena halves, streams and the
-    descriptor tables of the trace (built once on the device)."""
+    """The device side: pinned rings, the pool (or the resident device ring),
+    the scratch of the native loop, and the descriptor tables of the trace for
+    the offline comparison."""
 
     def __init__(self, trace: Trace, hbm_budget_bytes: int = 16 << 30, device=None, pivot: int = PIVOT_PARTIAL,
-                 seed: int = 0, resident: bool = False):
+                 seed: int = 0, resident: bool = False, max_batch: int | None = None):
         import torch
 
         from . import _lib
@@ -146,16 +118,21 @@ class CudaServer:
         self.trace = trace
         self.pivot = pivot
         total = trace.total_floats
-        # the pool: two halves, each at most half the budget and no larger than the whole trace
-        half = min(hbm_budget_bytes // 8, (total + 3) // 4 * 4)
-        half = max(half, int(trace.floats.max()) + 4)
-        if 8 * half > hbm_budget_bytes:
-            raise ValueError("the largest request does not fit the HBM budget")
-        self.half_floats = int(half)
-        # resident: the requests' matrices already sit in HBM (an upstream
-        # device stage produced them) and are inverted in place, no copies
+        largest = int(((trace.floats + 3) // 4 * 4).max()) if len(trace.k) else 0
         self.resident = resident
-        self.arena = None if resident else torch.empty(2 * self.half_floats, dtype=torch.float32, device=self.dev)
+        if resident:
+            # the upstream stage's device ring holds the requests: it is the
+            # server's memory for them and must fit the budget
+            if 4 * total > hbm_budget_bytes:
+                raise ValueError("the resident request ring does not fit the HBM budget")
+            self.pool_floats = 0
+            self.pool = None
+        else:
+            # the pool: the budget, or less when the whole trace needs less
+            self.pool_floats = int(min(hbm_budget_bytes // 4, (total + 3) // 4 * 4))
+            if largest > self.pool_floats:
+                raise ValueError("the largest request does not fit the HBM budget")
+            self.pool = torch.empty(self.pool_floats, dtype=torch.float32, device=self.dev)
         # host rings (pinned): requests in arrival order, uniform [-1, 1)
         g = torch.Generator(device=self.dev).manual_seed(seed)
         src = torch.empty(total, dtype=torch.float32, device=self.dev)
@@ -170,116 +147,65 @@ class CudaServer:
             self.ring_dev = src                       # inverted in place, restored before each run
             self.pristine = src.clone()
         del src
-        # descriptor tables of every matrix of the trace, in ring order, on the device
+        # most matrices in one coalesced launch: with host copies a batch waits
+        # for all its inputs, so moderate batches keep latency down; resident
+        # batches have no copies to wait for and amortise better when large
+        if max_batch is None:
+            max_batch = (1 << 20) if resident else (1 << 16)
+        self.max_batch = int(max(int(trace.k.max()) if len(trace.k) else 1, min(int(trace.k.sum()), max_batch)))
+        self.scratch = torch.empty(int(self.L.mi_serve_scratch_bytes(self.max_batch)), dtype=torch.uint8,
+                                   device=self.dev)
+        # descriptor tables of every matrix of the trace, in ring order (offline comparison)
         k, n, off = trace.k, trace.n, trace.offset
         req_of = np.repeat(np.arange(len(k)), k)
         first = np.concatenate([[0], np.cumsum(k)[:-1]])
         local = np.arange(int(k.sum())) - np.repeat(first, k)
         mat_off = off[req_of] + local * (n[req_of] ** 2)
-        self.mat_first = first.astype(np.int64)
         self.d_off = torch.from_numpy(mat_off.astype(np.int64)).to(self.dev)
         self.d_n = torch.from_numpy(n[req_of].astype(np.int32)).to(self.dev)
         self.d_flag = torch.full((int(k.sum()),), pivot, dtype=torch.int32, device=self.dev)
-        self.d_rel = torch.empty_like(self.d_off)          # batch-relative offsets, written per batch
         self.d_info = torch.zeros(int(k.sum()), dtype=torch.int32, device=self.dev)
         self.ws = torch.empty(max(int(self.L.mi_descr_workspace_bytes(int(k.sum()))), 256), dtype=torch.uint8,
                               device=self.dev)
-        self.s_h2d = torch.cuda.Stream(self.dev)
         self.s_cmp = torch.cuda.Stream(self.dev)
-        self.s_d2h = torch.cuda.Stream(self.dev)
         self.n_mask = 0
         for v in np.unique(n):
             self.n_mask |= 1 << (int(v) - 1)
+        self.last_stats = None
 
-    def _launch_batch(self, i: int, j: int, half: int, coalesce: bool):
+    def run(self, trace: Trace | None = None, coalesce: bool = True):
+        """Serve `trace` in real time through the native loop; returns
+        per-request latencies (s) and the wall time from the first arrival to
+        the last completion."""
         torch = self.torch
-        t = self.trace
-        base = int(t.offset[i])
-        end = int(t.offset[j - 1] + t.floats[j - 1])
-        span = end - base
-        if self.resident:
-            dst = self.ring_dev[base:end]
-        else:
-            dst = self.arena[half * self.half_floats: half * self.half_floats + span]
-            ev_in = torch.cuda.Event()
-            with torch.cuda.stream(self.s_h2d):
-                dst.copy_(self.ring_in[base:end], non_blocking=True)
-                ev_in.record(self.s_h2d)
-            self.s_cmp.wait_event(ev_in)
-        st = ctypes.c_void_p(self.s_cmp.cuda_stream)
-        m0 = int(self.mat_first[i])
-        m1 = int(self.mat_first[j - 1] + t.k[j - 1])
-        with torch.cuda.stream(self.s_cmp):
-            nb = t.n[i:j]
-            packed = bool(np.all(t.offset[i + 1:j] == t.offset[i:j - 1] + t.floats[i:j - 1]))
-            if coalesce and nb.min() == nb.max() and packed:
-                # one size, back to back in the ring: a single contiguous launch
-                status = self.L.mi_inverse_f32(ctypes.c_void_p(dst.data_ptr()), None,
-                                               ctypes.c_void_p(self.d_info[m0:m1].data_ptr()), m1 - m0, int(nb[0]),
-                                               self.pivot, st)
-                self.check(status)
-            elif coalesce:
-                offs = torch.sub(self.d_off[m0:m1], base, out=self.d_rel[m0:m1])
-                status = self.L.mi_inverse_descr_f32(
-                    ctypes.c_void_p(dst.data_ptr()), dst.numel(), ctypes.c_void_p(offs.data_ptr()),
-                    ctypes.c_void_p(self.d_n[m0:m1].data_ptr()), ctypes.c_void_p(self.d_flag[m0:m1].data_ptr()),
-                    None, ctypes.c_void_p(self.d_info[m0:m1].data_ptr()), m1 - m0, self.n_mask, 1 << self.pivot,
-                    ctypes.c_void_p(self.ws.data_ptr()), self.ws.numel(), st)
-                self.check(status)
-            else:
-                for r in range(i, j):
-                    o = int(t.offset[r]) - base
-                    nr = int(t.n[r])
-                    mr = int(self.mat_first[r])
-                    status = self.L.mi_inverse_f32(ctypes.c_void_p(dst.data_ptr() + 4 * o), None,
-                                                   ctypes.c_void_p(self.d_info[mr:mr + int(t.k[r])].data_ptr()),
-                                                   int(t.k[r]), nr, self.pivot, st)
-                    self.check(status)
-            ev_cmp = torch.cuda.Event()
-            ev_cmp.record(self.s_cmp)
-        if self.resident:
-            return ev_cmp
-        self.s_d2h.wait_event(ev_cmp)
-        ev_out = torch.cuda.Event()
-        with torch.cuda.stream(self.s_d2h):
-            self.ring_out[base:end].copy_(dst, non_blocking=True)
-            ev_out.record(self.s_d2h)
-        return ev_out
-
-    def run(self, trace: Trace | None = None, coalesce: bool = True, max_requests: int | None = None):
-        """Serve `trace` in real time; returns per-request latencies (s) and the
-        wall time from the first arrival to the last completion."""
         t = trace or self.trace
         assert np.array_equal(t.offset, self.trace.offset)
-        batcher = Batcher(t, self.half_floats, max_requests=(max_requests if coalesce else 1))
         nreq = len(t.k)
-        done = np.full(nreq, np.nan)
-        inflight: list[tuple[int, int, int, object]] = []   # (i, j, half, event)
-        free = [0, 1]
-        i = 0
-        completed = 0
-        push, pop = nvtx_ranges()
+        arrival = np.ascontiguousarray(t.arrival, dtype=np.float64)
+        kk = np.ascontiguousarray(t.k, dtype=np.int64)
+        nn = np.ascontiguousarray(t.n, dtype=np.int32)
+        off = np.ascontiguousarray(t.offset, dtype=np.int64)
+        lat = np.empty(nreq, dtype=np.float64)
+        wall = ctypes.c_double(0.0)
+        stats = np.zeros(2, dtype=np.int64)
         if self.resident:
             self.ring_dev.copy_(self.pristine)
-        self.torch.cuda.synchronize(self.dev)
-        t0 = time.perf_counter()
-        while completed < nreq:
-            now = time.perf_counter() - t0
-            while inflight and inflight[0][3].query():
-                a, b, h, _ = inflight.pop(0)
-                done[a:b] = now
-                completed += b - a
-                free.append(h)
-            if free and i < nreq and t.arrival[i] <= now:
-                j = batcher.next_batch(i, now)
-                h = free.pop(0)
-                push(f"batch requests {i}-{j - 1}")
-                inflight.append((i, j, h, self._launch_batch(i, j, h, coalesce)))
-                pop()
-                i = j
-        lat = done - t.arrival
-        wall = float(np.nanmax(done))
-        return lat, wall
+        torch.cuda.synchronize(self.dev)
+        push, pop = nvtx_ranges()
+        push(f"mi_serve_run {nreq} requests")
+        p = lambda a: ctypes.c_void_p(a.ctypes.data)
+        with torch.cuda.device(self.dev):
+            status = self.L.mi_serve_run(
+                nreq, p(arrival), p(kk), p(nn), p(off), ctypes.c_void_p(self.ring_in.data_ptr()),
+                ctypes.c_void_p(self.ring_out.data_ptr()),
+                ctypes.c_void_p(self.ring_dev.data_ptr() if self.resident else 0),
+                ctypes.c_void_p(self.pool.data_ptr() if self.pool is not None else 0), self.pool_floats,
+                ctypes.c_void_p(self.scratch.data_ptr()), self.scratch.numel(), self.max_batch, self.pivot,
+                1 if coalesce else 0, p(lat), ctypes.byref(wall), p(stats))
+        pop()
+        self.check(status)
+        self.last_stats = {"batches": int(stats[0]), "peak_pool_bytes": int(stats[1]) * 4}
+        return lat, float(wall.value)
 
     def results(self, r: int):
         """Output matrices of request r (host copy of the output ring)."""
@@ -333,9 +259,10 @@ def residual_max(A: np.ndarray, X: np.ndarray) -> float:
 
 
 def sweep(rates, num_requests: int, budget_gb: float = 16.0, seed: int = 0, modes=("coalesced", "per_request"),
-          resident: bool = False):
+          resident: bool = False, max_batch: int | None = None):
     base = make_trace(num_requests, rates[0], seed=seed)
-    srv = CudaServer(base, hbm_budget_bytes=int(budget_gb * (1 << 30)), seed=seed, resident=resident)
+    srv = CudaServer(base, hbm_budget_bytes=int(budget_gb * (1 << 30)), seed=seed, resident=resident,
+                     max_batch=max_batch)
     out = []
     matrices = int(base.k.sum())
     srv.run(retime(base, rates[0], seed), coalesce=True)        # warm-up: module load, occupancy caches
@@ -345,7 +272,7 @@ def sweep(rates, num_requests: int, budget_gb: float = 16.0, seed: int = 0, mode
     for rate in rates:
         tr = retime(base, rate, seed)
         row = {"rate_rps": rate, "requests": num_requests, "matrices": matrices, "resident": resident,
-               "offline_matrices_per_s": plain}
+               "offline_matrices_per_s": plain, "max_batch": srv.max_batch}
         outs = {}
         for mode in modes:
             lat, wall = srv.run(tr, coalesce=(mode == "coalesced"))
@@ -353,7 +280,7 @@ def sweep(rates, num_requests: int, budget_gb: float = 16.0, seed: int = 0, mode
             outs[mode] = {int(r): srv.results(r).copy() for r in sample[:4]}
             row[mode] = {"p50_ms": float(np.percentile(lat, 50) * 1e3), "p99_ms": float(np.percentile(lat, 99) * 1e3),
                          "matrices_per_s": matrices / wall, "requests_per_s": num_requests / wall,
-                         "max_residual_sample": res}
+                         "max_residual_sample": res, **srv.last_stats}
         if len(modes) == 2:
             row["equal_bits"] = all(np.array_equal(outs[modes[0]][r], outs[modes[1]][r]) for r in outs[modes[0]])
         out.append(row)
@@ -369,8 +296,11 @@ def main(argv=None):
     p.add_argument("--seed", type=int, default=0)
     p.add_argument("--out", default=None)
     p.add_argument("--resident", action="store_true", help="requests already in HBM: no host copies")
+    p.add_argument("--max-batch", type=int, default=None,
+                   help="most matrices in one coalesced launch (default 2^20 resident, 2^16 with copies)")
     a = p.parse_args(argv)
-    rows = sweep([float(x) for x in a.rates.split(",")], a.requests, a.budget_gb, a.seed, resident=a.resident)
+    rows = sweep([float(x) for x in a.rates.split(",")], a.requests, a.budget_gb, a.seed, resident=a.resident,
+                 max_batch=a.max_batch)
     if a.out:
         with open(a.out, "w") as f:
             json.dump(rows, f, indent=1)
