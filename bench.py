@@ -269,7 +269,7 @@ def main():
     e2e = None
     e2e_launches = 0
     if not args.no_e2e:
-        pipe = HostPipeline(n, chunk=65536, streams=3, device=dev)
+        pipe = HostPipeline(n, chunk=65536, streams=4, device=dev)
         hA = torch.from_numpy(host).pin_memory()
         hX = torch.empty_like(hA).pin_memory()
         hP = torch.empty((batch, n), dtype=torch.int32).pin_memory()
@@ -283,10 +283,18 @@ def main():
         barrier()
         dt = time.perf_counter() - t0
         dt = shards.max_over_ranks(dt, device=dev)
+        h2d_bytes = batch * n * n * 4
+        d2h_bytes = batch * n * n * 4 + batch * n * 4 + batch * 4
+        from matrixinversion_gb300.host import link_bandwidth
+
+        link = link_bandwidth(dev)
+        # both directions overlap, each at the rate they reach together
+        floor_ms = max(h2d_bytes, d2h_bytes) / (link["both_each_way_gbs"] * 1e9) * 1e3
+        step_ms = dt / e2e_steps * 1e3
         e2e = {"value": shards.aggregate_rate(batch * e2e_steps, dt, world), "unit": UNIT,
-               "h2d_bytes_per_step": batch * n * n * 4,
-               "d2h_bytes_per_step": batch * n * n * 4 + batch * n * 4 + batch * 4,
-               "steps": e2e_steps, "chunk_matrices": 65536, "streams": 3}
+               "h2d_bytes_per_step": h2d_bytes, "d2h_bytes_per_step": d2h_bytes,
+               "steps": e2e_steps, "chunk_matrices": 65536, "slots": 4, "ms_per_step": step_ms,
+               "link": {**link, "floor_ms": floor_ms, "frac": floor_ms / step_ms}}
         e2e_launches = pipe.launches_per_call(batch) * e2e_steps
 
     peak, peak_kind = hbm_peak()
