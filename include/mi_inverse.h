@@ -252,6 +252,42 @@ int mi_refine_df_next_f32(const float* d_a, float* d_x, const int32_t* d_list, i
                           float tol, int32_t* d_next, void* stream);
 
 /*
+ * As mi_refine_df_f32 for n = 32, with the residual R = I - A X formed on the
+ * tensor cores by error-free splitting: rows of A and columns of X cut into
+ * base-256 integer digits held exactly in bf16, digit products summed exactly
+ * in the FP32 accumulators of mma.sync and combined in float-float.  Groups
+ * of digit products up to 2^-37 of the row-times-column scale are always
+ * summed, up to 2^-45 when max|A| max|X| >= 2^12; the correction X R takes
+ * two-term bf16 splits of X and R.  d_a and d_x 16-byte aligned; n other than
+ * 32 -> MI_ERR_INVALID_VALUE.  No counterpart in the reference.
+ */
+int mi_refine_tc_f32(const float* d_a, float* d_x, const int32_t* d_list, int64_t count, int64_t batch, int n,
+                     void* stream);
+
+/*
+ * As mi_refine_tc_f32, and also writes d_next[t] = d_list[t] where the error
+ * left after this step, estimated as max|C R| / max|X| (C = X R, the
+ * correction), exceeds tol or is not finite, else -1 (also -1 for skipped
+ * entries).  d_next has count entries and may be d_list itself.  No
+ * counterpart in the reference.
+ */
+int mi_refine_tc_next_f32(const float* d_a, float* d_x, const int32_t* d_list, int64_t count, int64_t batch, int n,
+                          float tol, int32_t* d_next, void* stream);
+
+/*
+ * The flag and the first step of the refined form in one pass over the batch:
+ * for every b in [0, batch) whose condition estimate ||A_b||_1 ||X_b||_1 is
+ * at least flag_threshold (or not finite) -- the estimate
+ * mi_flag_condition_f32 computes, summed in another order -- one step of
+ * mi_refine_tc_next_f32; d_next[b] = b where that step leaves an estimated
+ * error above tol, else -1 (also -1 for matrices not refined).  d_next (batch
+ * entries, or NULL) is the list for a second mi_refine_tc_f32 step.  No
+ * counterpart in the reference.
+ */
+int mi_refine_tc_flagged_f32(const float* d_a, float* d_x, int64_t batch, int n, float flag_threshold, float tol,
+                             int32_t* d_next, void* stream);
+
+/*
  * d_list[b] = b if ||A_b||_1 * ||X_b||_1 >= threshold (or is not finite),
  * else -1, for b in [0, batch): a list the two refinement calls take as it is
  * (count = batch; -1 entries are skipped), so flagging needs no host round

@@ -89,6 +89,12 @@ def load(path: str | None = None):
     L.mi_refine_df_f32.restype = i32
     L.mi_refine_df_next_f32.argtypes = [vp, vp, vp, i64, i64, i32, ctypes.c_float, vp, vp]
     L.mi_refine_df_next_f32.restype = i32
+    L.mi_refine_tc_f32.argtypes = [vp, vp, vp, i64, i64, i32, vp]
+    L.mi_refine_tc_f32.restype = i32
+    L.mi_refine_tc_next_f32.argtypes = [vp, vp, vp, i64, i64, i32, ctypes.c_float, vp, vp]
+    L.mi_refine_tc_next_f32.restype = i32
+    L.mi_refine_tc_flagged_f32.argtypes = [vp, vp, i64, i32, ctypes.c_float, ctypes.c_float, vp, vp]
+    L.mi_refine_tc_flagged_f32.restype = i32
     L.mi_flag_condition_f32.argtypes = [vp, vp, i64, i32, ctypes.c_float, vp, vp]
     L.mi_flag_condition_f32.restype = i32
     L.mi_descr_workspace_bytes.argtypes = [i64]
@@ -126,6 +132,9 @@ def exported_symbols() -> list[str]:
         "mi_refine_fp64_f32",
         "mi_refine_df_f32",
         "mi_refine_df_next_f32",
+        "mi_refine_tc_f32",
+        "mi_refine_tc_next_f32",
+        "mi_refine_tc_flagged_f32",
         "mi_flag_condition_f32",
         "mi_set_launch_config",
         "mi_get_launch_config",

@@ -87,6 +87,34 @@ def refine_fp64_(A, X, index, stream=None):
     return X
 
 
+def _refine_step(prefix, A, X, index, stream, next_tol, next_out, max_n=32):
+    import torch
+
+    _check_pair(A, X)
+    _check_list("index", index, A.device)
+    n = A.shape[-1]
+    if n > max_n:
+        raise ValueError(f"{prefix} refinement takes n <= {max_n}")
+    st = (stream or torch.cuda.current_stream(A.device)).cuda_stream
+    lib = _lib.load()
+    step = getattr(lib, f"mi_refine_{prefix}_f32")
+    step_next = getattr(lib, f"mi_refine_{prefix}_next_f32")
+    with torch.cuda.device(A.device):
+        if next_tol is None:
+            status = step(ctypes.c_void_p(A.data_ptr()), ctypes.c_void_p(X.data_ptr()),
+                          ctypes.c_void_p(index.data_ptr()), index.numel(), A.shape[0], n, ctypes.c_void_p(st))
+            _lib.check(status)
+            return X
+        if next_out is None:
+            next_out = torch.empty_like(index)
+        _check_list("next_out", next_out, A.device, index.numel())
+        status = step_next(ctypes.c_void_p(A.data_ptr()), ctypes.c_void_p(X.data_ptr()),
+                           ctypes.c_void_p(index.data_ptr()), index.numel(), A.shape[0], n, float(next_tol),
+                           ctypes.c_void_p(next_out.data_ptr()), ctypes.c_void_p(st))
+    _lib.check(status)
+    return next_out
+
+
 def refine_df_(A, X, index, stream=None, next_tol=None, next_out=None):
     """One refinement step with a float-float residual for the matrices
     X[index] (in place): the accuracy of the FP64 step at FP32-pipe speed.
@@ -96,27 +124,38 @@ def refine_df_(A, X, index, stream=None, next_tol=None, next_out=None):
     max|X R^2| / max|X| (X, R = I - A X before the step), exceeds next_tol,
     else -1.  next_out (CUDA int32, index.numel() entries) receives it and may
     be `index` itself."""
+    return _refine_step("df", A, X, index, stream, next_tol, next_out)
+
+
+def refine_tc_(A, X, index, stream=None, next_tol=None, next_out=None):
+    """As refine_df_ for 32 x 32 matrices, with the residual formed exactly on
+    the tensor cores (base-256 digits in bf16, exact FP32 group sums, float-
+    float combination) and the correction X R from two-term bf16 splits; the
+    second-step estimate is max|C R| / max|X| with C = X R the correction."""
+    return _refine_step("tc", A, X, index, stream, next_tol, next_out)
+
+
+def refine_tc_flagged_(A, X, flag_threshold: float = REFINE_FLAG, next_tol: float = REFINE_TOL, next_out=None,
+                       stream=None):
+    """The flag and the first tensor-core step in one pass (32 x 32 only):
+    every matrix whose condition estimate ||A||_1 ||X||_1 is at least
+    flag_threshold (or not finite) gets one refine_tc_ step, in place.
+    Returns the full-length CUDA int32 list for a second step: b where the
+    step leaves an estimated error above next_tol, else -1."""
     import torch
 
     _check_pair(A, X)
-    _check_list("index", index, A.device)
-    n = A.shape[-1]
+    batch, n = A.shape[0], A.shape[-1]
+    if n != 32:
+        raise ValueError("the fused flag-and-step pass takes n = 32")
+    if next_out is None:
+        next_out = torch.empty(batch, dtype=torch.int32, device=A.device)
+    _check_list("next_out", next_out, A.device, batch)
     st = (stream or torch.cuda.current_stream(A.device)).cuda_stream
-    lib = _lib.load()
     with torch.cuda.device(A.device):
-        if next_tol is None:
-            status = lib.mi_refine_df_f32(ctypes.c_void_p(A.data_ptr()), ctypes.c_void_p(X.data_ptr()),
-                                          ctypes.c_void_p(index.data_ptr()), index.numel(), A.shape[0], n,
-                                          ctypes.c_void_p(st))
-            _lib.check(status)
-            return X
-        if next_out is None:
-            next_out = torch.empty_like(index)
-        _check_list("next_out", next_out, A.device, index.numel())
-        status = lib.mi_refine_df_next_f32(ctypes.c_void_p(A.data_ptr()), ctypes.c_void_p(X.data_ptr()),
-                                           ctypes.c_void_p(index.data_ptr()), index.numel(), A.shape[0], n,
-                                           float(next_tol), ctypes.c_void_p(next_out.data_ptr()),
-                                           ctypes.c_void_p(st))
+        status = _lib.load().mi_refine_tc_flagged_f32(ctypes.c_void_p(A.data_ptr()), ctypes.c_void_p(X.data_ptr()),
+                                                      batch, n, float(flag_threshold), float(next_tol),
+                                                      ctypes.c_void_p(next_out.data_ptr()), ctypes.c_void_p(st))
     _lib.check(status)
     return next_out
 
@@ -153,20 +192,33 @@ def flag_list(A, X, threshold: float = 1e4, out=None):
     return out
 
 
-def refined_inverse(A, flag_threshold: float = REFINE_FLAG, tol: float = REFINE_TOL, lists: bool = False):
+def refined_inverse(A, flag_threshold: float = REFINE_FLAG, tol: float = REFINE_TOL, lists: bool = False,
+                    step: str = "auto"):
     """The refined form of batched_inverse(A, "partial"): the FP32
-    partial-pivoting inverse, one float-float-residual step for every matrix
-    whose condition estimate ||A||_1 ||X||_1 is at least flag_threshold, and a
-    second step only where the first leaves an estimated error above tol.
-    Flags and lists stay on the device (no host round trip).  Returns
-    (X, perm, info), plus the first and second step lists if `lists`."""
+    partial-pivoting inverse, one refinement step with a residual accurate
+    beyond FP32 for every matrix whose condition estimate ||A||_1 ||X||_1 is
+    at least flag_threshold, and a second step only where the first leaves an
+    estimated error above tol.  step: "tc" (residual on the tensor cores,
+    n = 32 only), "df" (float-float on the FP32 pipes, any n), or "auto" ("tc"
+    at n = 32, else "df").  Flags and lists stay on the device (no host round
+    trip).  Returns (X, perm, info), plus the first and second step lists if
+    `lists`."""
     import matrixinversion_gb300 as mi
 
+    if step == "auto":
+        step = "tc" if A.shape[-1] == 32 else "df"
+    if step not in ("tc", "df"):
+        raise ValueError(f"unknown refinement step {step!r}")
     X, perm, info = mi.batched_inverse(A, "partial")
-    ix = flag_list(A, X, threshold=flag_threshold)
-    first = ix.clone() if lists else None
-    refine_df_(A, X, ix, next_tol=tol, next_out=ix)
-    refine_df_(A, X, ix)
+    first = flag_list(A, X, threshold=flag_threshold) if (lists or step == "df") else None
+    if step == "tc":
+        # flag and first step fused: one pass over A and X fewer
+        ix = refine_tc_flagged_(A, X, flag_threshold, tol)
+        refine_tc_(A, X, ix)
+    else:
+        ix = first.clone() if lists else first
+        refine_df_(A, X, ix, next_tol=tol, next_out=ix)
+        refine_df_(A, X, ix)
     return (X, perm, info, first, ix) if lists else (X, perm, info)
 
 
@@ -215,26 +267,29 @@ def study(per_bucket: int = 65536, kappas=KAPPAS, steps=(1, 2), seed: int = 0, t
         refine_fp64_(A, X, idx)
         e = rel_error(X, X64)
         row["ns1_fp64_flagged"] = {"median": float(e.median()), "max": float(e.max()), "flagged": int(idx.numel())}
-        # float-float residual steps on the flagged matrices, from the plain inverse
-        for nsteps in (1, 2):
-            X = X0.clone()
-            idx = flag_ill_conditioned(A, X)
-            for _ in range(nsteps):
-                refine_df_(A, X, idx)
-            e = rel_error(X, X64)
-            row[f"df{nsteps}_flagged"] = {"median": float(e.median()), "max": float(e.max()),
-                                          "flagged": int(idx.numel())}
-        # the refined form (refined_inverse), timed end to end on a fresh copy
-        _, _, _, first, second = refined_inverse(A, lists=True)
-        torch.cuda.synchronize()
-        ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
-        ev[0].record()
-        Xref, _, _ = refined_inverse(A)
-        ev[1].record()
-        torch.cuda.synchronize()
-        ms = ev[0].elapsed_time(ev[1])
-        e = rel_error(Xref, X64)
-        row["refined"] = {"median": float(e.median()), "max": float(e.max()), "flagged": int((first >= 0).sum()),
+        # float-float and tensor-core residual steps on the flagged matrices,
+        # from the plain inverse
+        for name, fn in (("df", refine_df_), ("tc", refine_tc_)):
+            for nsteps in (1, 2):
+                X = X0.clone()
+                idx = flag_ill_conditioned(A, X)
+                for _ in range(nsteps):
+                    fn(A, X, idx)
+                e = rel_error(X, X64)
+                row[f"{name}{nsteps}_flagged"] = {"median": float(e.median()), "max": float(e.max()),
+                                                  "flagged": int(idx.numel())}
+        # the refined form (refined_inverse) with either step, timed end to end
+        for label, step in (("refined", "tc"), ("refined_df", "df")):
+            _, _, _, first, second = refined_inverse(A, lists=True, step=step)
+            torch.cuda.synchronize()
+            ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+            ev[0].record()
+            Xref, _, _ = refined_inverse(A, step=step)
+            ev[1].record()
+            torch.cuda.synchronize()
+            ms = ev[0].elapsed_time(ev[1])
+            e = rel_error(Xref, X64)
+            row[label] = {"median": float(e.median()), "max": float(e.max()), "flagged": int((first >= 0).sum()),
                           "second_step": int((second >= 0).sum()), "ms": ms,
                           "matrices_per_s": per_bucket / ms * 1e3}
         # the reference pivot rule's inverse, plain and after one NS step
@@ -255,7 +310,9 @@ def study(per_bucket: int = 65536, kappas=KAPPAS, steps=(1, 2), seed: int = 0, t
                       ("ns1", lambda X: newton_schulz_(A, X, 1)), ("ns2", lambda X: newton_schulz_(A, X, 2)),
                       ("fp64_all", lambda X: refine_fp64_(A, X, all_idx)),
                       ("df_all", lambda X: refine_df_(A, X, all_idx)),
-                      ("df_all_with_estimate", lambda X: refine_df_(A, X, all_idx, next_tol=REFINE_TOL))):
+                      ("df_all_with_estimate", lambda X: refine_df_(A, X, all_idx, next_tol=REFINE_TOL)),
+                      ("tc_all", lambda X: refine_tc_(A, X, all_idx)),
+                      ("tc_all_with_estimate", lambda X: refine_tc_(A, X, all_idx, next_tol=REFINE_TOL))):
         bufs = [(A if label.startswith("inverse") else X0).clone() for _ in range(timing_iters + 2)]
         for b in bufs[:2]:
             fn(b)
@@ -299,13 +356,53 @@ def bench_ns(count: int = 262144, steps: int = 1, iters: int = 5, seed: int = 0)
             "GBs": count * 12288 * steps / ms / 1e6}
 
 
+def bench_refined(count: int = 262144, iters: int = 5, seed: int = 0):
+    """Throughput of the plain partial-pivoting inverse and of the refined
+    form with either step on `count` uniform [-1, 1) 32 x 32 matrices (every
+    one flagged: their condition estimates are far above 8), CUDA events on
+    the current stream, fresh inputs per iteration (each batch 4 MB x count /
+    1024, above L2 at the default size)."""
+    import torch
+
+    import matrixinversion_gb300 as mi
+
+    g = torch.Generator(device="cuda").manual_seed(seed)
+    As = [torch.rand(count, 32, 32, generator=g, device="cuda") * 2 - 1 for _ in range(2)]
+    out = {"count": count}
+    for label, fn in (("plain_partial", lambda A: mi.batched_inverse(A, "partial")),
+                      ("refined_tc", lambda A: refined_inverse(A, step="tc")),
+                      ("refined_df", lambda A: refined_inverse(A, step="df"))):
+        for i in range(2):
+            fn(As[i % 2])
+        torch.cuda.synchronize()
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        ev[0].record()
+        for i in range(iters):
+            fn(As[i % 2])
+        ev[1].record()
+        torch.cuda.synchronize()
+        ms = ev[0].elapsed_time(ev[1]) / iters
+        out[label] = {"ms": ms, "matrices_per_s": count / ms * 1e3}
+    _, _, _, first, second = refined_inverse(As[0], lists=True)
+    out["flagged"] = int((first >= 0).sum())
+    out["second_step"] = int((second >= 0).sum())
+    out["tc_vs_plain"] = out["plain_partial"]["ms"] / out["refined_tc"]["ms"]
+    out["df_vs_plain"] = out["plain_partial"]["ms"] / out["refined_df"]["ms"]
+    return out
+
+
 def main(argv=None):
     p = argparse.ArgumentParser()
     p.add_argument("--per-bucket", type=int, default=65536)
     p.add_argument("--seed", type=int, default=0)
     p.add_argument("--out", default=None)
     p.add_argument("--ns-only", type=int, default=0, help="only time the Newton-Schulz kernel on this many matrices")
+    p.add_argument("--refined-only", type=int, default=0,
+                   help="only time the refined form against the plain inverse on this many matrices")
     a = p.parse_args(argv)
+    if a.refined_only:
+        print(json.dumps(bench_refined(a.refined_only, seed=a.seed)), flush=True)
+        return
     if a.ns_only:
         for k in (1, 2):
             print(json.dumps(bench_ns(a.ns_only, k, seed=a.seed)), flush=True)

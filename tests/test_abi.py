@@ -201,6 +201,19 @@ def test_noalloc_and_descriptor_argument_checks_without_gpu(lib):
         assert f(None, None, None, 0, 4, 32, None) == _lib.MI_OK
         assert f(None, None, None, 4, 4, 32, None) == _lib.MI_ERR_NULL_POINTER
     assert lib.mi_refine_df_next_f32(p, p, p, 4, 4, 32, -1.0, p, None) == _lib.MI_ERR_INVALID_VALUE
+    f = lib.mi_refine_tc_f32
+    assert f(None, None, None, 4, 4, 16, None) == _lib.MI_ERR_INVALID_VALUE          # n = 32 only
+    assert f(None, None, None, 0, 4, 32, None) == _lib.MI_OK
+    assert f(None, None, None, 4, 4, 32, None) == _lib.MI_ERR_NULL_POINTER
+    assert f(ctypes.c_void_p(0x100004), p, p, 4, 4, 32, None) == _lib.MI_ERR_MISALIGNED
+    assert lib.mi_refine_tc_next_f32(p, p, p, 4, 4, 32, -1.0, p, None) == _lib.MI_ERR_INVALID_VALUE
+    g = lib.mi_refine_tc_flagged_f32
+    assert g(p, p, 4, 31, 8.0, 3e-7, p, None) == _lib.MI_ERR_INVALID_VALUE
+    assert g(p, p, 4, 32, float("nan"), 3e-7, p, None) == _lib.MI_ERR_INVALID_VALUE
+    assert g(p, p, 4, 32, 8.0, -1.0, p, None) == _lib.MI_ERR_INVALID_VALUE
+    assert g(None, None, 0, 32, 8.0, 3e-7, None, None) == _lib.MI_OK
+    assert g(None, p, 4, 32, 8.0, 3e-7, p, None) == _lib.MI_ERR_NULL_POINTER
+    assert g(p, ctypes.c_void_p(0x100008), 4, 32, 8.0, 3e-7, p, None) == _lib.MI_ERR_MISALIGNED
     assert lib.mi_flag_condition_f32(None, None, 4, 0, 8.0, None, None) == _lib.MI_ERR_INVALID_VALUE
     assert lib.mi_flag_condition_f32(None, None, 4, 32, 8.0, None, None) == _lib.MI_ERR_NULL_POINTER
 

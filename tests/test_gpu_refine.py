@@ -257,3 +257,127 @@ def test_refined_inverse_reaches_1e6(mi_gpu, oracle):
         assert int((first >= 0).sum()) == 256
         if kappa < 1e4:
             assert int((second >= 0).sum()) == 0
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kappa", [1e1, 1e3, 1e5, 1e6])
+def test_tensor_core_step_matches_its_restatement(mi_gpu, kappa):
+    """mi_refine_tc_f32 against its CPU restatement (tests/test_refine_design.py):
+    the digit groups are exact integers and the float-float combination runs in
+    the same order, so R is the same bits; only the tensor core's summation
+    order in C = X R differs, so X + C agrees to within 4 units in the last
+    place of max|X|.  Out-of-range list entries leave their matrices as they
+    were."""
+    import torch
+
+    from matrixinversion_gb300 import refine
+    from test_refine_design import _tc_step
+
+    A = _inputs(kappa, 96, 71)
+    X0, _, _ = mi_gpu.batched_inverse(A, "partial")
+    idx = torch.arange(A.shape[0], dtype=torch.int32, device="cuda")
+    idx[10] = -1
+    idx[20] = A.shape[0] + 7
+    X1 = X0.clone()
+    refine.refine_tc_(A, X1, idx)
+    torch.cuda.synchronize()
+    a, x0, x1 = A.cpu().numpy(), X0.cpu().numpy(), X1.cpu().numpy()
+    want = _tc_step(a, x0)[0]
+    assert np.array_equal(x1[10], x0[10]) and np.array_equal(x1[20], x0[20])
+    live = [b for b in range(A.shape[0]) if b not in (10, 20)]
+    diff = np.abs(x1[live].astype(np.float64) - want[live]).max((1, 2)) / np.abs(want[live]).max((1, 2))
+    assert diff.max() <= 2.0 ** -22, diff.max()
+
+
+@pytest.mark.gpu
+def test_tensor_core_second_step_estimate(mi_gpu, oracle):
+    """mi_refine_tc_next_f32: the step is bit-identical to mi_refine_tc_f32;
+    a matrix left off the second-step list has error <= tol + 1e-7; skipped
+    and non-finite entries behave; the list may overwrite the index array."""
+    import torch
+
+    from matrixinversion_gb300 import refine
+
+    tol = 3e-7
+    A = torch.cat([_inputs(1e3, 64, 81), _inputs(1e5, 448, 82)])
+    X0, _, _ = mi_gpu.batched_inverse(A, "partial")
+    X0[7] = float("nan")
+    batch = A.shape[0]
+    idx = torch.arange(batch, dtype=torch.int32, device="cuda")
+    idx[5] = -1
+    idx[9] = batch + 3
+    X64, _, _ = oracle.inverse_f64(A.cpu().numpy(), "partial")
+    Xa = X0.clone()
+    refine.refine_tc_(A, Xa, idx)
+    Xb = X0.clone()
+    nxt = refine.refine_tc_(A, Xb, idx, next_tol=tol)
+    Xc = X0.clone()
+    lst = idx.clone()
+    same = refine.refine_tc_(A, Xc, lst, next_tol=tol, next_out=lst)
+    torch.cuda.synchronize()
+    assert same.data_ptr() == lst.data_ptr()
+    assert torch.equal(Xa.view(torch.int32), Xb.view(torch.int32))
+    assert torch.equal(Xb.view(torch.int32), Xc.view(torch.int32))
+    nx = nxt.cpu().numpy()
+    assert np.array_equal(nx, lst.cpu().numpy())
+    assert nx[5] == -1 and nx[9] == -1 and nx[7] == 7
+    ix = idx.cpu().numpy()
+    assert all(v in (-1, ix[t]) for t, v in enumerate(nx))
+    x = Xb.cpu().numpy().astype(np.float64)
+    err = np.abs(x - X64).max((1, 2)) / np.abs(X64).max((1, 2))
+    keep = [b for b in range(batch) if b not in (5, 7, 9) and nx[b] == -1]
+    assert len(keep) > batch // 2
+    assert err[keep].max() <= tol + 1e-7, err[keep].max()
+    assert all(nx[b] == -1 for b in range(64) if b != 7)
+
+
+@pytest.mark.gpu
+def test_refined_inverse_both_steps_reach_1e6_up_to_kappa_1e6(mi_gpu, oracle):
+    """The refined form with either step -- the residual on the tensor cores
+    (the default at n = 32) or in float-float on the FP32 pipes -- meets
+    max |X - X64| <= 1e-6 max |X64| per matrix in every bucket up to
+    kappa = 1e6."""
+    import torch
+
+    from matrixinversion_gb300 import refine
+
+    for kappa, seed in ((1e1, 91), (1e4, 92), (1e6, 93)):
+        A = _inputs(kappa, 256, seed)
+        X64, _, _ = oracle.inverse_f64(A.cpu().numpy(), "partial")
+        for step in ("tc", "df"):
+            X, _, info = refine.refined_inverse(A, step=step)
+            torch.cuda.synchronize()
+            assert (info.cpu().numpy() == 0).all()
+            x = X.cpu().numpy().astype(np.float64)
+            err = np.abs(x - X64).max((1, 2)) / np.abs(X64).max((1, 2))
+            assert err.max() <= 1e-6, (kappa, step, err.max())
+
+
+@pytest.mark.gpu
+def test_fused_flag_and_step_equals_flag_then_step(mi_gpu):
+    """mi_refine_tc_flagged_f32 (flag and first step in one pass) gives the
+    same bits and the same second-step list as mi_flag_condition_f32 followed
+    by mi_refine_tc_next_f32, on a batch whose condition estimates sit far on
+    either side of the threshold (kappa 10 below 1e4, kappa 1e5 above); a NaN
+    inverse is flagged and listed; matrices below the threshold are left as
+    they were."""
+    import torch
+
+    from matrixinversion_gb300 import refine
+
+    A = torch.cat([_inputs(1e1, 96, 101), _inputs(1e5, 160, 102)])
+    X0, _, _ = mi_gpu.batched_inverse(A, "partial")
+    X0[100] = float("nan")
+    thr, tol = 1e4, 3e-7
+    Xa = X0.clone()
+    lst = refine.flag_list(A, Xa, threshold=thr)
+    nxt_a = refine.refine_tc_(A, Xa, lst, next_tol=tol)
+    Xb = X0.clone()
+    nxt_b = refine.refine_tc_flagged_(A, Xb, thr, tol)
+    torch.cuda.synchronize()
+    assert torch.equal(Xa.view(torch.int32), Xb.view(torch.int32))
+    assert torch.equal(nxt_a, nxt_b)
+    f = lst.cpu().numpy()
+    assert (f[:96] == -1).all() and (f[96:] >= 0).all()
+    assert torch.equal(Xb[:96].view(torch.int32), X0[:96].view(torch.int32))
+    assert int(nxt_b[100]) == 100

@@ -129,3 +129,119 @@ def test_refined_form_meets_1e6_in_every_bucket(buckets):
             X2[listed], _, _ = _df_step(A[listed], X1[listed])
         e2 = _rel_err(X2, X64)
         assert e2.max() <= 1e-6, (kappa, e2.max(), int(listed.sum()))
+
+
+# ---------------------------------------------------------------------------
+# The tensor-core step (mi_refine_tc_kernel), restated on the CPU: rows of A
+# and columns of X scaled by powers of two to below 256 and cut into digits
+# on the grids 2^(-8s) (round to nearest by adding and subtracting
+# 1.5 * 2^(23 - 8s) in FP32, exact in bf16), digit-product groups d = s + t
+# summed exactly (the kernel's FP32 tensor-core accumulators; float64 here,
+# where the sums are exact too), combined by TwoSum in FP32 and scaled back,
+# R rounded once; the correction C = X R from two-term bf16 splits of X and R.
+
+DIGITS, LOW_GROUPS, DEEP_EXP = 6, 5, 12
+
+
+def _bf16(x):
+    """Round FP32 to bf16 (nearest, ties to even), returned as FP32."""
+    u = np.ascontiguousarray(x, dtype=F).view(np.uint32).astype(np.uint64)
+    u = (u + 0x7FFF + ((u >> 16) & 1)) & 0xFFFF0000
+    return u.astype(np.uint32).view(F)
+
+
+def _line_exp(mx):
+    """e with mx < 2^e (frexp's exponent; 0 for 0), clamped to [-100, 120]."""
+    return np.clip(np.frexp(mx.astype(F))[1], -100, 120).astype(np.int64)
+
+
+def _digits(M, inv_scale, ndig):
+    v = (M * inv_scale).astype(F)                        # exact: powers of two
+    out = []
+    for s in range(ndig):
+        c = F(1.5 * 2.0 ** (23 - 8 * s))
+        q = ((v + c) - c).astype(F)                      # v rounded to a multiple of 2^(-8s)
+        assert np.array_equal(_bf16(q), q)               # 8 significant bits at most
+        out.append(q.astype(np.float64))
+        v = (v - q).astype(F)                            # exact
+    return out
+
+
+def _tc_step(A, X, tol=None):
+    B, n, _ = A.shape
+    ea = _line_exp(np.abs(A).max(axis=2))                # [B, n] rows of A
+    ex = _line_exp(np.abs(X).max(axis=1))                # [B, n] columns of X
+    deep = ea.max(axis=1) + ex.max(axis=1) >= DEEP_EXP
+    sa = np.ldexp(F(1), ea - 8).astype(F)[:, :, None]
+    sx = np.ldexp(F(1), ex - 8).astype(F)[:, None, :]
+    ad = _digits(A, np.ldexp(F(1), 8 - ea).astype(F)[:, :, None], DIGITS)
+    xd = _digits(X, np.ldexp(F(1), 8 - ex).astype(F)[:, None, :], DIGITS)
+    hi = np.zeros((B, n, n), F)
+    lo = np.zeros((B, n, n), F)
+    gmax = 0.0
+    for d in range(DIGITS):
+        G = sum(np.einsum("bik,bkj->bij", ad[s], xd[d - s]) for s in range(d + 1))
+        gmax = max(gmax, float(np.abs(G * 2.0 ** (8 * d)).max()))          # in units of the grid 2^(-8d)
+        p = G.astype(F)
+        assert np.array_equal(p.astype(np.float64), G)                      # exact in FP32
+        if d >= LOW_GROUPS:
+            p = np.where(deep[:, None, None], p, F(0))
+        if d == 0:
+            hi = p
+        else:
+            hi, r = _two_sum(hi, p)
+            lo = (lo + r).astype(F)
+    s2 = (sa * sx).astype(F)
+    R = ((np.eye(n, dtype=F) - (hi * s2).astype(F)) - (lo * s2).astype(F)).astype(F)
+    rh = _bf16(R)
+    rl = _bf16(R - rh)
+    xh = _bf16(X)
+    xl = _bf16(X - xh)
+    f64 = lambda M: M.astype(np.float64)
+    C = (np.einsum("bik,bkj->bij", f64(xh), f64(rh) + f64(rl))
+         + np.einsum("bik,bkj->bij", f64(xl), f64(rh))).astype(F)
+    Xn = (X + C).astype(F)
+    listed = None
+    if tol is not None:
+        e2 = np.einsum("bik,bkj->bij", f64(_bf16(C)), f64(rh)).astype(F)
+        listed = np.isnan(e2).any(axis=(1, 2)) | ~(np.abs(e2).max(axis=(1, 2)) <= F(tol) * np.abs(X).max(axis=(1, 2)))
+    return Xn, R, listed, deep, gmax
+
+
+def test_tc_groups_are_exact_and_the_residual_deep_enough(buckets):
+    """Every digit-product group stays below 2^22 units of its grid (exact in FP32); the
+    residual's error is below 2^-36 of the |A||X| scale with groups 0..4 and
+    below 2^-43 where the matrix takes group 5."""
+    for kappa, (A, X0, _) in buckets.items():
+        _, R, _, deep, gmax = _tc_step(A, X0)
+        assert gmax <= 2.0 ** 22                       # bound: 32 * (8 * 2^14) for group 5
+        exact = np.eye(32) - np.einsum("bik,bkj->bij", A.astype(np.float64), X0.astype(np.float64))
+        scale = np.einsum("bik,bkj->bij", np.abs(A.astype(np.float64)), np.abs(X0.astype(np.float64))).max((1, 2))
+        err = np.abs(R - exact) - np.abs(exact) * 2.0 ** -24   # less R's own final rounding
+        err = err.max((1, 2)) / scale
+        assert err[~deep].max(initial=0) < 2.0 ** -36, (kappa, err[~deep].max(initial=0))
+        assert err[deep].max(initial=0) < 2.0 ** -43, (kappa, err[deep].max(initial=0))
+        if kappa >= 1e5:
+            assert deep.all()
+        if kappa <= 1e1:
+            assert not deep.any()
+
+
+def test_tc_step_reaches_the_u_level_and_its_estimate_is_safe(buckets):
+    for kappa, (A, X0, X64) in buckets.items():
+        e0 = _rel_err(X0, X64)
+        X1, _, listed, _, _ = _tc_step(A, X0, tol=TOL)
+        e1 = _rel_err(X1, X64)
+        if kappa <= 1e5:
+            assert e1.max() < 0.05 * e0.max() + 2e-7, (kappa, e0.max(), e1.max())
+        assert np.all(e1[~listed] <= TOL + 5e-8), (kappa, e1[~listed].max())
+
+
+def test_tc_refined_form_meets_1e6_in_every_bucket(buckets):
+    for kappa, (A, X0, X64) in buckets.items():
+        X1, _, listed, _, _ = _tc_step(A, X0, tol=TOL)
+        X2 = X1.copy()
+        if listed.any():
+            X2[listed] = _tc_step(A[listed], X1[listed])[0]
+        e2 = _rel_err(X2, X64)
+        assert e2.max() <= 1e-6, (kappa, e2.max(), int(listed.sum()))
