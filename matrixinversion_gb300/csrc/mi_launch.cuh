@@ -213,7 +213,7 @@ LaunchForm launch_form(long long batch, int tpb) {
         if (batch >= tiny_min_batch<N, MODE>()) return {kFormThread, 1, 32, tiny_threads<N>()};
     }
     if constexpr (MODE == kModePartial && N >= kRowsMin && rows_partial_enabled<N>())
-        return {kFormRows, kRowsLanes, kRowsMats, 32 * kRowsWarps};
+        return {kFormRows, RowsGeom<N>::kLanes, RowsGeom<N>::kMats, 32 * kRowsWarps};
     if constexpr (N == WideGeom::N && MODE != kModePartial)
         return {kFormLanes, WideGeom::L, WideGeom::M, tpb < WideGeom::kThreadsMax ? tpb : WideGeom::kThreadsMax};
     constexpr int L = default_lanes(N, MODE);

@@ -6,22 +6,24 @@
 //     routines of matrix multiplication and its applications", Numer.
 //     Algorithms 59, 2012, restated here for bf16 tensor cores).  Row i of A
 //     is scaled by 2^(8 - ea_i), the power of two that brings its largest
-//     entry below 256, and cut into base-256 digits, each an integer in
-//     (-256, 256) and so exact in bf16; column j of X likewise with
-//     2^(8 - ex_j).  The FP32 scalings and digit cuts are exact.
-//   * Digit products summed over k = 0..31 stay below 32 * 255^2 < 2^21, and a
-//     group d = s + t (s, t digit indices) of at most six of them below
-//     6 * 2^21 < 2^24: every group is an exact integer in the FP32
-//     accumulators of mma.sync (bf16 inputs, FP32 accumulation), whatever
-//     order the tensor core adds in.  (A X)_ij = 2^(ea_i + ex_j - 16)
-//     sum_d 2^(-8 d) G_d[i][j], less the groups left out; the scaled groups
-//     (exact FP32 numbers) are summed in float-float (TwoSum) and
-//     R = (delta_ij - hi) - lo is rounded once.
+//     entry below 256, and cut into digits: digit s is the remainder rounded
+//     to a multiple of 2^(-8s), an integer in [-256, 256] (s = 0) or in
+//     [-128, 128] times 2^(-8s), so 8 significant bits, exact in bf16.
+//     Column j of X likewise with 2^(8 - ex_j).  Scalings and cuts are exact.
+//   * Digit products summed over k = 0..31 stay below 2^21 units of their
+//     grid 2^(-8(s+t)), and a group d = s + t of at most six of them below
+//     2^22 units: every group is an exact number in the FP32 accumulators of
+//     mma.sync (bf16 inputs, FP32 accumulation), whatever order the tensor
+//     core adds in.  (A X)_ij = 2^(ea_i + ex_j - 16) sum_d G_d[i][j], less the
+//     groups left out; R = (delta_ij - s hi) - s lo, rounded once, with
+//     s = 2^(ea_i + ex_j - 16) and hi + lo the float-float sum of the groups.
 //   * Groups 0..4 leave out less than about 2^-37 of max_i,j |A_i.| |X_.j|
-//     (rows and columns) -- enough while max|A| max|X| stays below about 2^12;
-//     above that the matrix takes group 5 too (2^-45): a warp-uniform branch,
-//     so well-conditioned matrices pay 15 digit products and ill-conditioned
-//     ones 21.
+//     (rows and columns); where max|A| max|X| may reach 2^16 the matrix takes
+//     group 5 too (a warp-uniform branch), so most matrices pay 15 digit
+//     products and very ill-conditioned ones 21.  Only G0 + G1 carry the
+//     cancellation of A X against I and are summed by TwoSum; the smaller
+//     groups are added to the low part, which rounds at about 2^-40 of the
+//     scale.
 //   * X <- X + C, C = X R with X and R each split into two bf16 terms
 //     (hi*hi + hi*lo + lo*hi, FP32 accumulation): C is small, so its 16 bits
 //     of relative accuracy are plenty.
@@ -50,7 +52,7 @@ namespace tcr {
 constexpr int kWarps = 4;                // matrices per block
 constexpr int kDigits = 6;               // base-256 digits per operand
 constexpr int kLowGroups = 5;            // groups every matrix takes
-constexpr int kDeepExp = 12;             // group 5 too when max|A| max|X| may reach 2^kDeepExp
+constexpr int kDeepExp = 16;             // group 5 too when max|A| max|X| may reach 2^kDeepExp
 constexpr int kTile = 32 * 32 * 2;       // bytes of one 32 x 32 bf16 tile
 
 struct WarpSmem {
@@ -85,10 +87,22 @@ __device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], 
         : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
 }
 
+// d = A B with no accumulator input (C = 0)
+__device__ __forceinline__ void mma_bf16_z(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
+    const float z = 0.0f;
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%10,%10,%10,%10};"
+        : "=f"(d[0]), "=f"(d[1]), "=f"(d[2]), "=f"(d[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1), "f"(z));
+}
+
 typedef float Frag[2][4][4];             // a lane's share of a 32 x 32 FP32 accumulator
 
-// acc += A_tile * B_tile, both swizzled 32 x 32 bf16 tiles in shared memory,
-// A row-major [i][k], B row-major [k][j].
+// acc (+)= A_tile * B_tile, both swizzled 32 x 32 bf16 tiles in shared
+// memory, A row-major [i][k], B row-major [k][j]; kInit: acc = the product
+// (its old value is not read).
+template <bool kInit = false>
 __device__ __forceinline__ void tile_mma(Frag& acc, uint32_t a, uint32_t b, int lane) {
     const int q = lane >> 3, r8 = lane & 7;
 #pragma unroll
@@ -102,11 +116,23 @@ __device__ __forceinline__ void tile_mma(Frag& acc, uint32_t a, uint32_t b, int 
             ldsm_x4_t(b + tofs(16 * kc + r8 + (q & 1) * 8, 16 * np + (q >> 1) * 8), bf);
 #pragma unroll
             for (int mt = 0; mt < 2; mt++) {
-                mma_bf16(acc[mt][2 * np], af[mt], bf[0], bf[1]);
-                mma_bf16(acc[mt][2 * np + 1], af[mt], bf[2], bf[3]);
+                if (kInit && kc == 0) {
+                    mma_bf16_z(acc[mt][2 * np], af[mt], bf[0], bf[1]);
+                    mma_bf16_z(acc[mt][2 * np + 1], af[mt], bf[2], bf[3]);
+                } else {
+                    mma_bf16(acc[mt][2 * np], af[mt], bf[0], bf[1]);
+                    mma_bf16(acc[mt][2 * np + 1], af[mt], bf[2], bf[3]);
+                }
             }
         }
     }
+}
+
+// acc = group d: the sum over u = 0..d of A digit u times X digit d - u
+__device__ __forceinline__ void group_sum(Frag& acc, uint32_t ad0, uint32_t xd0, int d, int lane) {
+    tile_mma<true>(acc, ad0, xd0 + d * kTile, lane);
+#pragma unroll 1
+    for (int u = 1; u <= d; u++) tile_mma(acc, ad0 + u * kTile, xd0 + (d - u) * kTile, lane);
 }
 
 __device__ __forceinline__ void zero(Frag& acc) {
@@ -319,35 +345,52 @@ __global__ void __launch_bounds__(32 * tcr::kWarps) mi_refine_tc_kernel(const fl
         }
         __syncwarp();
         if (live_n) load_rows(va, A + bn * 1024, lane);   // in flight during the products
-        // sum_d G_d in float-float, element pairs of the fragments on packed
-        // FP32x2 arithmetic; group d is an exact FP32 number on the grid
-        // 2^(-8d) (of the row's and column's scales)
+        // the sum of the groups in float-float, element pairs of the fragments
+        // on packed FP32x2 arithmetic (in units of the row's and column's
+        // scales).  G0 and G1 (below 2^22 units, exact) carry the cancellation
+        // of A X against I: TwoSum(G0, G1) = hi + lo exactly.  G2 (exact,
+        // below 2^6 units) is added to lo (rounding at 2^-18 units, about
+        // 2^-40 of the scale), and the groups from 3 up (below 2^-2 units)
+        // share one accumulator, whose additions round at 2^-26 units or less.
         float2 hi[2][4][2], lo[2][4][2];
         Frag acc;
-        zero(acc);
-        tile_mma(acc, ad0, xd0, lane);
+        group_sum(acc, ad0, xd0, 0, lane);                                         // G0
+#pragma unroll
+        for (int mt = 0; mt < 2; mt++)
+#pragma unroll
+            for (int nt = 0; nt < 4; nt++)
+#pragma unroll
+                for (int h = 0; h < 2; h++) hi[mt][nt][h] = make_float2(acc[mt][nt][2 * h], acc[mt][nt][2 * h + 1]);
+        group_sum(acc, ad0, xd0, 1, lane);                                         // G1
 #pragma unroll
         for (int mt = 0; mt < 2; mt++)
 #pragma unroll
             for (int nt = 0; nt < 4; nt++)
 #pragma unroll
                 for (int h = 0; h < 2; h++) {
-                    hi[mt][nt][h] = make_float2(acc[mt][nt][2 * h], acc[mt][nt][2 * h + 1]);
                     lo[mt][nt][h] = make_float2(0.0f, 0.0f);
+                    two_sum2(hi[mt][nt][h], lo[mt][nt][h], make_float2(acc[mt][nt][2 * h], acc[mt][nt][2 * h + 1]));
                 }
+        group_sum(acc, ad0, xd0, 2, lane);                                         // G2
+#pragma unroll
+        for (int mt = 0; mt < 2; mt++)
+#pragma unroll
+            for (int nt = 0; nt < 4; nt++)
+#pragma unroll
+                for (int h = 0; h < 2; h++)
+                    lo[mt][nt][h] = __fadd2_rn(lo[mt][nt][h], make_float2(acc[mt][nt][2 * h], acc[mt][nt][2 * h + 1]));
+        group_sum(acc, ad0, xd0, 3, lane);                                         // G3 + G4 (+ G5)
 #pragma unroll 1
-        for (int d = 1; d < ndig; d++) {
-            zero(acc);
+        for (int d = 4; d < ndig; d++)
 #pragma unroll 1
-            for (int s = 0; s <= d; s++) tile_mma(acc, ad0 + s * kTile, xd0 + (d - s) * kTile, lane);
+            for (int u = 0; u <= d; u++) tile_mma(acc, ad0 + u * kTile, xd0 + (d - u) * kTile, lane);
 #pragma unroll
-            for (int mt = 0; mt < 2; mt++)
+        for (int mt = 0; mt < 2; mt++)
 #pragma unroll
-                for (int nt = 0; nt < 4; nt++)
+            for (int nt = 0; nt < 4; nt++)
 #pragma unroll
-                    for (int h = 0; h < 2; h++)
-                        two_sum2(hi[mt][nt][h], lo[mt][nt][h], make_float2(acc[mt][nt][2 * h], acc[mt][nt][2 * h + 1]));
-        }
+                for (int h = 0; h < 2; h++)
+                    lo[mt][nt][h] = __fadd2_rn(lo[mt][nt][h], make_float2(acc[mt][nt][2 * h], acc[mt][nt][2 * h + 1]));
         __syncwarp();                                     // every digit read: the tiles are free
         // R = (delta - s hi) - s lo, s = 2^(ea_i + ex_j - 16) (exact products),
         // as two bf16 terms (operand B of X R); X as two bf16 terms (operand
@@ -389,8 +432,7 @@ __global__ void __launch_bounds__(32 * tcr::kWarps) mi_refine_tc_kernel(const fl
         // C = X R (three bf16 products), X <- X + C: C goes through shared
         // memory (FP32, swizzled) into row order, so that X + C is formed from
         // the registers and written as whole 512-byte rows
-        zero(acc);
-        tile_mma(acc, smem_addr(xh), smem_addr(rh), lane);
+        tile_mma<true>(acc, smem_addr(xh), smem_addr(rh), lane);
         tile_mma(acc, smem_addr(xh), smem_addr(rl), lane);
         tile_mma(acc, smem_addr(xl), smem_addr(rh), lane);
         float* cf = reinterpret_cast<float*>(sm.ad[2]);  // 4 KB: tiles 2 and 3
@@ -426,8 +468,7 @@ __global__ void __launch_bounds__(32 * tcr::kWarps) mi_refine_tc_kernel(const fl
                         put_bf16x2(ch, erow(mt, e, lane), ecol(nt, e, lane), acc[mt][nt][e], acc[mt][nt][e + 1]);
             __syncwarp();
             Frag e2;
-            zero(e2);
-            tile_mma(e2, smem_addr(ch), smem_addr(rh), lane);
+            tile_mma<true>(e2, smem_addr(ch), smem_addr(rh), lane);
             float emax = 0.0f;
             bool nan = false;
 #pragma unroll

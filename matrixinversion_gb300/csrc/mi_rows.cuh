@@ -27,15 +27,25 @@
 
 namespace mi {
 
-constexpr int kRowsLanes = 16;      // lanes per matrix
-constexpr int kRowsMats = 2;        // matrices per warp
-constexpr int kRowsWarps = 4;       // warps per block (3 blocks per SM at up to 170 registers)
+constexpr int kRowsWarps = 4;       // warps per block
 constexpr int kRowsMin = 16;        // smallest n of this kernel (partial pivoting)
 
+// Lanes per matrix at size n: 16 (two matrices per warp, two rows per lane)
+// or 8 (four matrices per warp, up to four rows per lane).  Measured on GB300
+// at 1,000,000 matrices, same bits: 8 lanes take n = 18 from 2.92 to 2.12 ms
+// but are slower at n = 17 (3.10 against 2.59 ms), 20, 22, 24 (4.62 against
+// 4.21) and far slower from n = 25 up, where four whole rows per lane spill
+// (n = 32: 12.04 against 6.74 ms).
 template <int N>
+__host__ __device__ constexpr int rows_lanes() { return N == 18 ? 8 : 16; }
+
+template <int N, int LN = rows_lanes<N>()>
 struct RowsGeom {
     static_assert(N >= 1 && N <= 32, "n must be in 1..32");
-    static constexpr int R = (N + kRowsLanes - 1) / kRowsLanes;     // rows per lane
+    static_assert(LN == 8 || LN == 16, "8 or 16 lanes per matrix");
+    static constexpr int kLanes = LN;                               // lanes per matrix
+    static constexpr int kMats = 32 / LN;                           // matrices per warp
+    static constexpr int R = (N + LN - 1) / LN;                     // rows per lane
     static constexpr int NC = (N + 3) & ~3;                         // register columns
     static constexpr int SP = (((N + 3) / 4) | 1) * 4;              // stage row pitch (floats)
     static constexpr int kMat = N * SP;                             // stage floats per matrix
@@ -46,8 +56,8 @@ struct RowsGeom {
     static constexpr int oWin = oD + 32;
     static constexpr int oMap = oWin + 32;
     static constexpr int kScr = oMap + 32;
-    static constexpr int oScr = kRowsMats * kMat;                   // scratch after the stage
-    static constexpr int kWarp = (oScr + kRowsMats * kScr + 31) & ~31;   // floats per warp (128-byte multiple)
+    static constexpr int oScr = kMats * kMat;                       // scratch after the stage
+    static constexpr int kWarp = (oScr + kMats * kScr + 31) & ~31;  // floats per warp (128-byte multiple)
     static_assert(kMat % 4 == 0 && kScr % 4 == 0 && NC % 4 == 0, "16-byte alignment of rows and buffers");
 };
 
@@ -62,26 +72,27 @@ __device__ __forceinline__ unsigned rows_key(float x) {
     return (b > 0x7f800000u) ? 1u : b + 2u;
 }
 
-// Maximum over the 16 lanes of this lane's group (xor offsets < 16 stay in
+// Maximum over the LN lanes of this lane's group (xor offsets < LN stay in
 // the group).  Measured: one redux.sync per group mask instead (both groups
-// of a warp in one instruction) is 6-10% slower here.
+// of a warp in one instruction) is 6-10% slower here at 16 lanes.
+template <int LN>
 __device__ __forceinline__ unsigned rows_group_max(unsigned v) {
 #pragma unroll
-    for (int o = 8; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(kFull, v, o));
+    for (int o = LN / 2; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(kFull, v, o));
     return v;
 }
 
-template <int N>
-__global__ void __launch_bounds__(32 * kRowsWarps, 3) mi_rows_partial_kernel(float* __restrict__ A,
-                                                                            int32_t* __restrict__ perm_out,
-                                                                            int32_t* __restrict__ info_out,
-                                                                            long long batch, int vec) {
-    using G = RowsGeom<N>;
+template <int N, int LN = rows_lanes<N>()>
+__global__ void __launch_bounds__(32 * kRowsWarps, LN == 16 ? 3 : 2) mi_rows_partial_kernel(
+    float* __restrict__ A, int32_t* __restrict__ perm_out, int32_t* __restrict__ info_out, long long batch, int vec) {
+    using G = RowsGeom<N, LN>;
     constexpr int R = G::R, NC = G::NC, SP = G::SP, NN = N * N;
+    constexpr int kRowsLanes = G::kLanes, kRowsMats = G::kMats;
+    constexpr unsigned kGroupMask = (1u << kRowsLanes) - 1u;
     extern __shared__ float4 rows_smem[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     float* ws = reinterpret_cast<float*>(rows_smem) + warp * G::kWarp;
-    const int mslot = lane >> 4, s = lane & 15, gbase = mslot * kRowsLanes;
+    const int mslot = lane / kRowsLanes, s = lane % kRowsLanes, gbase = mslot * kRowsLanes;
     float* st = ws + mslot * G::kMat;                    // this lane's matrix in the stage
     float* scr = ws + G::oScr + mslot * G::kScr;
     int* win = reinterpret_cast<int*>(scr + G::oWin);
@@ -155,9 +166,9 @@ __global__ void __launch_bounds__(32 * kRowsWarps, 3) mi_rows_partial_kernel(flo
                     bs = s + kRowsLanes * ri;
                 }
             }
-            const unsigned mx = rows_group_max(bk);
+            const unsigned mx = rows_group_max<kRowsLanes>(bk);
             const unsigned cand = (bk != 0u && bk == mx) ? (((unsigned)(255 - bl) << 8) | (unsigned)bs) : 0u;
-            const unsigned best = rows_group_max(cand);
+            const unsigned best = rows_group_max<kRowsLanes>(cand);
             const int r = (int)(best & 0xffu);               // pivot slot
             const int lw = 255 - (int)(best >> 8);           // its logical row
 #pragma unroll
@@ -275,7 +286,7 @@ __global__ void __launch_bounds__(32 * kRowsWarps, 3) mi_rows_partial_kernel(flo
         for (int ri = 0; ri < R; ri++) {
             const int t = s + kRowsLanes * ri;
             const bool z = valid && t < N && scr[G::oD + t] == 0.0f;
-            zmask |= ((__ballot_sync(kFull, z) >> gbase) & 0xffffu) << (kRowsLanes * ri);
+            zmask |= ((__ballot_sync(kFull, z) >> gbase) & kGroupMask) << (kRowsLanes * ri);
             if (valid && t < N && perm_out != nullptr) perm_out[(b0 + mslot) * N + t] = win[t];
         }
         if (valid && s == 0 && info_out != nullptr) info_out[b0 + mslot] = zmask ? __ffs(zmask) : 0;
@@ -289,6 +300,7 @@ template <int N>
 cudaError_t launch_rows_partial(float* a, int32_t* perm, int32_t* info, long long batch, int grid,
                                 cudaStream_t stream) {
     using G = RowsGeom<N>;
+    constexpr int kRowsMats = G::kMats;
     constexpr int threads = 32 * kRowsWarps;
     constexpr size_t smem = (size_t)kRowsWarps * G::kWarp * sizeof(float);
     auto kern = mi_rows_partial_kernel<N>;

@@ -391,6 +391,56 @@ def bench_refined(count: int = 262144, iters: int = 5, seed: int = 0):
     return out
 
 
+def config4(per_bucket: int = 65536, kappas=KAPPAS, seed: int = 0, iters: int = 5):
+    """The precision configuration as one batch: the kappa buckets
+    (per_bucket matrices each, 262,144 in all by default) concatenated into a
+    single [batch, 32, 32] tensor, inverted plain (partial pivoting) and in the
+    refined form with either step, each as one call over the whole batch.
+    Per bucket: median and max relative error against the FP64 inverse; for
+    the batch: kernel-path time (CUDA events, mean of `iters` calls after one
+    warm-up) and matrices/s, and the refined form's rate as a fraction of the
+    plain kernel's at the same batch."""
+    import torch
+
+    import matrixinversion_gb300 as mi
+
+    A = torch.cat([conditioned(per_bucket, k, seed=seed + i) for i, k in enumerate(kappas)])
+    X64 = torch.cat([torch.linalg.inv(A[i * per_bucket:(i + 1) * per_bucket].double())
+                     for i in range(len(kappas))])
+    batch = A.shape[0]
+    out = {"batch": batch, "per_bucket": per_bucket, "buckets": []}
+    runs = {"plain_partial": lambda: mi.batched_inverse(A, "partial")[0],
+            "refined_tc": lambda: refined_inverse(A, step="tc")[0],
+            "refined_df": lambda: refined_inverse(A, step="df")[0]}
+    errs, timing = {}, {}
+    for label, fn in runs.items():
+        X = fn()
+        torch.cuda.synchronize()
+        errs[label] = rel_error(X, X64)
+        del X
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        ev[0].record()
+        for _ in range(iters):
+            fn()
+        ev[1].record()
+        torch.cuda.synchronize()
+        ms = ev[0].elapsed_time(ev[1]) / iters
+        timing[label] = {"ms": ms, "matrices_per_s": batch / ms * 1e3}
+    _, _, _, first, second = refined_inverse(A, lists=True)
+    for i, k in enumerate(kappas):
+        sl = slice(i * per_bucket, (i + 1) * per_bucket)
+        row = {"kappa": k}
+        for label, e in errs.items():
+            row[label] = {"median": float(e[sl].median()), "max": float(e[sl].max())}
+        row["flagged"] = int((first[sl] >= 0).sum())
+        row["second_step"] = int((second[sl] >= 0).sum())
+        out["buckets"].append(row)
+    out["timing"] = timing
+    out["refined_tc_vs_plain"] = timing["plain_partial"]["ms"] / timing["refined_tc"]["ms"]
+    out["refined_df_vs_plain"] = timing["plain_partial"]["ms"] / timing["refined_df"]["ms"]
+    return out
+
+
 def main(argv=None):
     p = argparse.ArgumentParser()
     p.add_argument("--per-bucket", type=int, default=65536)
@@ -399,7 +449,16 @@ def main(argv=None):
     p.add_argument("--ns-only", type=int, default=0, help="only time the Newton-Schulz kernel on this many matrices")
     p.add_argument("--refined-only", type=int, default=0,
                    help="only time the refined form against the plain inverse on this many matrices")
+    p.add_argument("--config4", action="store_true",
+                   help="the kappa buckets as one batch: errors per bucket and the refined form's rate")
     a = p.parse_args(argv)
+    if a.config4:
+        r = config4(a.per_bucket, seed=a.seed)
+        print(json.dumps(r), flush=True)
+        if a.out:
+            with open(a.out, "w") as f:
+                json.dump(r, f, indent=1)
+        return
     if a.refined_only:
         print(json.dumps(bench_refined(a.refined_only, seed=a.seed)), flush=True)
         return

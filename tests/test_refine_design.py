@@ -136,11 +136,13 @@ def test_refined_form_meets_1e6_in_every_bucket(buckets):
 # and columns of X scaled by powers of two to below 256 and cut into digits
 # on the grids 2^(-8s) (round to nearest by adding and subtracting
 # 1.5 * 2^(23 - 8s) in FP32, exact in bf16), digit-product groups d = s + t
-# summed exactly (the kernel's FP32 tensor-core accumulators; float64 here,
-# where the sums are exact too), combined by TwoSum in FP32 and scaled back,
-# R rounded once; the correction C = X R from two-term bf16 splits of X and R.
+# summed in the kernel's FP32 tensor-core accumulators (exactly for groups
+# 0..2; groups 3 and up share one accumulator) and combined as the kernel
+# does: TwoSum(G0, G1), then G2 and the rest added to the low part, scaled
+# back, R rounded once; the correction C = X R from two-term bf16 splits of X
+# and R.
 
-DIGITS, LOW_GROUPS, DEEP_EXP = 6, 5, 12
+DIGITS, LOW_GROUPS, DEEP_EXP = 6, 5, 16
 
 
 def _bf16(x):
@@ -176,21 +178,25 @@ def _tc_step(A, X, tol=None):
     sx = np.ldexp(F(1), ex - 8).astype(F)[:, None, :]
     ad = _digits(A, np.ldexp(F(1), 8 - ea).astype(F)[:, :, None], DIGITS)
     xd = _digits(X, np.ldexp(F(1), 8 - ex).astype(F)[:, None, :], DIGITS)
-    hi = np.zeros((B, n, n), F)
-    lo = np.zeros((B, n, n), F)
     gmax = 0.0
+    G = []
     for d in range(DIGITS):
-        G = sum(np.einsum("bik,bkj->bij", ad[s], xd[d - s]) for s in range(d + 1))
-        gmax = max(gmax, float(np.abs(G * 2.0 ** (8 * d)).max()))          # in units of the grid 2^(-8d)
-        p = G.astype(F)
-        assert np.array_equal(p.astype(np.float64), G)                      # exact in FP32
+        g = sum(np.einsum("bik,bkj->bij", ad[s], xd[d - s]) for s in range(d + 1))
+        gmax = max(gmax, float(np.abs(g * 2.0 ** (8 * d)).max()))          # in units of the grid 2^(-8d)
+        if d < 3:
+            assert np.array_equal(g.astype(F).astype(np.float64), g)         # groups 0..2 exact in FP32
         if d >= LOW_GROUPS:
-            p = np.where(deep[:, None, None], p, F(0))
-        if d == 0:
-            hi = p
-        else:
-            hi, r = _two_sum(hi, p)
-            lo = (lo + r).astype(F)
+            g = np.where(deep[:, None, None], g, 0.0)
+        G.append(g)
+    # TwoSum(G0, G1) = hi + lo exactly; lo += G2; lo += the groups from 3 up,
+    # which the kernel sums in one tensor-core accumulator (rounded here once
+    # per group, the accumulator's order aside)
+    hi, lo = _two_sum(G[0].astype(F), G[1].astype(F))
+    lo = (lo + G[2].astype(F)).astype(F)
+    tail = G[3].astype(F)
+    for g in G[4:]:
+        tail = (tail + g.astype(F)).astype(F)
+    lo = (lo + tail).astype(F)
     s2 = (sa * sx).astype(F)
     R = ((np.eye(n, dtype=F) - (hi * s2).astype(F)) - (lo * s2).astype(F)).astype(F)
     rh = _bf16(R)
@@ -209,9 +215,11 @@ def _tc_step(A, X, tol=None):
 
 
 def test_tc_groups_are_exact_and_the_residual_deep_enough(buckets):
-    """Every digit-product group stays below 2^22 units of its grid (exact in FP32); the
-    residual's error is below 2^-36 of the |A||X| scale with groups 0..4 and
-    below 2^-43 where the matrix takes group 5."""
+    """Every digit-product group stays below 2^22 units of its grid (groups
+    0..2, summed alone, are exact in FP32); the residual's error is below 2^-36
+    of the |A||X| scale with groups 0..4 and below 2^-39 where the matrix takes
+    group 5 (there the additions to the low part, G2 up to 2^6 units, round at
+    about 2^-40 of the scale)."""
     for kappa, (A, X0, _) in buckets.items():
         _, R, _, deep, gmax = _tc_step(A, X0)
         assert gmax <= 2.0 ** 22                       # bound: 32 * (8 * 2^14) for group 5
@@ -220,10 +228,10 @@ def test_tc_groups_are_exact_and_the_residual_deep_enough(buckets):
         err = np.abs(R - exact) - np.abs(exact) * 2.0 ** -24   # less R's own final rounding
         err = err.max((1, 2)) / scale
         assert err[~deep].max(initial=0) < 2.0 ** -36, (kappa, err[~deep].max(initial=0))
-        assert err[deep].max(initial=0) < 2.0 ** -43, (kappa, err[deep].max(initial=0))
-        if kappa >= 1e5:
-            assert deep.all()
-        if kappa <= 1e1:
+        assert err[deep].max(initial=0) < 2.0 ** -39, (kappa, err[deep].max(initial=0))
+        if kappa >= 1e6:
+            assert deep.mean() > 0.9
+        if kappa <= 1e5:
             assert not deep.any()
 
 
@@ -245,3 +253,24 @@ def test_tc_refined_form_meets_1e6_in_every_bucket(buckets):
             X2[listed] = _tc_step(A[listed], X1[listed])[0]
         e2 = _rel_err(X2, X64)
         assert e2.max() <= 1e-6, (kappa, e2.max(), int(listed.sum()))
+
+
+def test_pivot_growth_cannot_flag_ill_conditioning(buckets):
+    """Why the refined form flags by the condition estimate ||A||_1 ||X||_1
+    and not by pivot growth max|U| / max|A| (U from partial-pivoting LU, as
+    the elimination forms it): with partial pivoting the growth stays O(1) in
+    every kappa bucket -- the ill-conditioned buckets do not grow more -- so
+    no growth threshold separates kappa = 1e1 (FP32 error ~1e-6) from
+    kappa = 1e6 (~1e-2); the estimate tracks kappa within a small factor."""
+    sl = pytest.importorskip("scipy.linalg")
+    growth, est = {}, {}
+    for kappa, (A, X0, _) in buckets.items():
+        g = []
+        for b in range(64):
+            _, _, U = sl.lu(A[b].astype(np.float64))
+            g.append(np.abs(U).max() / np.abs(A[b]).max())
+        growth[kappa] = np.array(g)
+        est[kappa] = np.abs(A).sum(1).max(1) * np.abs(X0).sum(1).max(1)
+    assert growth[1e6].max() < growth[1e1].max() and growth[1e6].min() < 1.0 < growth[1e1].max()
+    for kappa, e in est.items():
+        assert np.all(e >= kappa) and np.all(e <= 64 * kappa), (kappa, e.min(), e.max())
