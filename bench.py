@@ -274,19 +274,26 @@ def main():
         hX = torch.empty_like(hA).pin_memory()
         hP = torch.empty((batch, n), dtype=torch.int32).pin_memory()
         hI = torch.empty((batch,), dtype=torch.int32).pin_memory()
+        from matrixinversion_gb300.host import link_bandwidth
+
         pipe.run(hA, args.pivot, hX, hP, hI)
+        # the link's rates just before and just after the timed steps: the
+        # host memory behind the link is shared with whatever else runs on the
+        # machine, and a rate that drops during the run shows up here
+        link_before = link_bandwidth(dev)
         e2e_steps = max(1, min(args.steps, 5))
+        step_times = []
         barrier()
         t0 = time.perf_counter()
         for _ in range(e2e_steps):
+            t1 = time.perf_counter()
             pipe.run(hA, args.pivot, hX, hP, hI)
+            step_times.append((time.perf_counter() - t1) * 1e3)
         barrier()
         dt = time.perf_counter() - t0
         dt = shards.max_over_ranks(dt, device=dev)
         h2d_bytes = batch * n * n * 4
         d2h_bytes = batch * n * n * 4 + batch * n * 4 + batch * 4
-        from matrixinversion_gb300.host import link_bandwidth
-
         link = link_bandwidth(dev)
         # both directions overlap, each at the rate they reach together
         floor_ms = max(h2d_bytes, d2h_bytes) / (link["both_each_way_gbs"] * 1e9) * 1e3
@@ -294,7 +301,9 @@ def main():
         e2e = {"value": shards.aggregate_rate(batch * e2e_steps, dt, world), "unit": UNIT,
                "h2d_bytes_per_step": h2d_bytes, "d2h_bytes_per_step": d2h_bytes,
                "steps": e2e_steps, "chunk_matrices": 65536, "slots": 4, "ms_per_step": step_ms,
-               "link": {**link, "floor_ms": floor_ms, "frac": floor_ms / step_ms}}
+               "step_ms": [round(t, 2) for t in step_times],
+               "link": {**link, "floor_ms": floor_ms, "frac": floor_ms / step_ms,
+                        "before": link_before}}
         e2e_launches = pipe.launches_per_call(batch) * e2e_steps
 
     peak, peak_kind = hbm_peak()
