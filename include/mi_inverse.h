@@ -253,12 +253,13 @@ int mi_refine_df_next_f32(const float* d_a, float* d_x, const int32_t* d_list, i
 
 /*
  * As mi_refine_df_f32 for n = 32, with the residual R = I - A X formed on the
- * tensor cores by error-free splitting: rows of A and columns of X cut into
- * base-256 integer digits held exactly in bf16, digit products summed exactly
- * in the FP32 accumulators of mma.sync and combined in float-float.  Groups
- * of digit products up to 2^-37 of the row-times-column scale are always
- * summed, up to 2^-45 when max|A| max|X| >= 2^12; the correction X R takes
- * two-term bf16 splits of X and R.  d_a and d_x 16-byte aligned; n other than
+ * tensor cores by error-free splitting: rows of A and columns of X, scaled by
+ * powers of two, cut into digits of 8 significant bits held exactly in bf16,
+ * digit products grouped so that each group is exact in the FP32 accumulators
+ * of mma.sync, the groups combined in float-float.  The residual carries about
+ * 37 bits of the row-times-column scale (about 40 where max|A| max|X| may
+ * reach 2^16 and a sixth digit is taken); the correction X R takes two-term
+ * bf16 splits of X and R.  d_a and d_x 16-byte aligned; n other than
  * 32 -> MI_ERR_INVALID_VALUE.  No counterpart in the reference.
  */
 int mi_refine_tc_f32(const float* d_a, float* d_x, const int32_t* d_list, int64_t count, int64_t batch, int n,
