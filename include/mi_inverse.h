@@ -34,6 +34,9 @@
  *   mi_set_launch_config / mi_get_launch_config  the NUMTHREADS table of
  *                       parallel_pivot/run.py:187-224, per (n, pivot), settable
  *                       at run time (by the autotuner).
+ *   mi_set_launch_lanes / mi_get_launch_lanes  lanes per matrix per (n, pivot),
+ *                       tuned likewise (no reference counterpart: its launch
+ *                       uses one thread per column).
  */
 #ifndef MI_INVERSE_H
 #define MI_INVERSE_H
@@ -305,6 +308,20 @@ int mi_flag_condition_f32(const float* d_a, const float* d_x, int64_t batch, int
  */
 int mi_set_launch_config(int n, int pivot, int threads_per_block);
 int mi_get_launch_config(int n, int pivot, int* threads_per_block);
+
+/*
+ * Lanes per matrix for size n and pivot mode (the width of the sub-warp that
+ * owns a matrix; the reference fixes one thread per column,
+ * parallel_pivot/luBatchedInplace.cu:4-11).  Sizes 17..31 without partial
+ * pivoting run at 16 or 8 lanes -- the same bits either way -- and ship with
+ * the choice measured on GB300; every other (n, pivot) has one width.  Set
+ * lanes_per_matrix to that width, the alternative, or 0 to restore the table's
+ * entry; anything else -> MI_ERR_INVALID_VALUE.  mi_get_launch_lanes returns
+ * the installed width and the alternative (0 if none).  Contiguous calls and
+ * descriptor buckets both follow the entry.
+ */
+int mi_set_launch_lanes(int n, int pivot, int lanes_per_matrix);
+int mi_get_launch_lanes(int n, int pivot, int* lanes_per_matrix, int* alternative);
 
 const char* mi_error_string(int status);
 /* Text of the last CUDA error seen by this thread ("" if none). */

@@ -103,6 +103,10 @@ def load(path: str | None = None):
     L.mi_set_launch_config.restype = i32
     L.mi_get_launch_config.argtypes = [i32, i32, ip]
     L.mi_get_launch_config.restype = i32
+    L.mi_set_launch_lanes.argtypes = [i32, i32, i32]
+    L.mi_set_launch_lanes.restype = i32
+    L.mi_get_launch_lanes.argtypes = [i32, i32, ip, ip]
+    L.mi_get_launch_lanes.restype = i32
     _lib = L
     return L
 
@@ -138,6 +142,8 @@ def exported_symbols() -> list[str]:
         "mi_flag_condition_f32",
         "mi_set_launch_config",
         "mi_get_launch_config",
+        "mi_set_launch_lanes",
+        "mi_get_launch_lanes",
         "mi_set_wait_test",
         "mi_serve_scratch_bytes",
         "mi_serve_run",

@@ -50,8 +50,8 @@ bool register_device_error_reader(device_error_reader fn) {
 
 // Threads per block per (n, pivot mode), measured on GB300 by the autotuner
 // (matrixinversion_gb300/autotune.py: 262,144 uniform matrices per size, the
-// fastest of 32..256; reference_serial uses the reference column); 0 = the
-// built-in default of 128.  mi_set_launch_config overrides entries at run
+// fastest of 32..256; n = 17..31 at the lanes per matrix of kLanesGB300);
+// 0 = the built-in default of 128.  mi_set_launch_config overrides entries at run
 // time (0 restores this table's entry).
 static const int kTunedGB300[33][4] = {
     {0, 0, 0, 0},
@@ -74,18 +74,18 @@ static const int kTunedGB300[33][4] = {
     {32, 256, 256, 256},
     {128, 256, 256, 256},
     {256, 256, 256, 256},
-    {32, 256, 256, 256},
+    {256, 256, 32, 256},
+    {256, 256, 256, 256},
+    {256, 256, 128, 256},
+    {256, 256, 256, 256},
+    {256, 256, 64, 256},
+    {256, 256, 32, 256},
+    {256, 256, 32, 256},
     {256, 256, 256, 256},
     {256, 256, 256, 256},
-    {256, 256, 256, 256},
-    {256, 256, 256, 256},
-    {128, 256, 256, 256},
-    {32, 256, 256, 256},
-    {128, 256, 256, 256},
-    {256, 256, 256, 256},
-    {128, 256, 256, 256},
-    {64, 256, 256, 256},
-    {64, 64, 64, 256},
+    {32, 256, 128, 256},
+    {128, 256, 128, 256},
+    {128, 256, 64, 256},
     {256, 256, 256, 256}};
 static int g_tuned[33][4];
 static bool g_tuned_init = [] {
@@ -93,6 +93,57 @@ static bool g_tuned_init = [] {
         for (int m = 0; m < 4; m++) g_tuned[n][m] = kTunedGB300[n][m];
     return true;
 }();
+
+// Lanes per matrix per (n, pivot mode), measured on GB300 by the autotuner
+// (262,144 uniform matrices per size, eight against sixteen lanes, the same
+// bits either way; eight where they were at least 2% faster); 0 =
+// default_lanes.  Only n = 17..31 without partial pivoting have a
+// choice (alt_lanes); mi_set_launch_lanes overrides entries at run time.
+static const int kLanesGB300[33][4] = {
+    {0, 0, 0, 0},
+    {0, 0, 0, 0},
+    {0, 0, 0, 0},
+    {0, 0, 0, 0},
+    {0, 0, 0, 0},
+    {0, 0, 0, 0},
+    {0, 0, 0, 0},
+    {0, 0, 0, 0},
+    {0, 0, 0, 0},
+    {0, 0, 0, 0},
+    {0, 0, 0, 0},
+    {0, 0, 0, 0},
+    {0, 0, 0, 0},
+    {0, 0, 0, 0},
+    {0, 0, 0, 0},
+    {0, 0, 0, 0},
+    {0, 0, 0, 0},
+    {8, 8, 0, 0},
+    {8, 8, 0, 0},
+    {8, 8, 0, 0},
+    {8, 8, 8, 0},
+    {8, 0, 0, 0},
+    {0, 0, 0, 0},
+    {8, 0, 0, 0},
+    {8, 0, 0, 0},
+    {8, 8, 8, 0},
+    {8, 8, 8, 0},
+    {8, 8, 8, 0},
+    {8, 8, 8, 0},
+    {0, 0, 0, 0},
+    {0, 0, 0, 0},
+    {0, 0, 0, 0},
+    {0, 0, 0, 0}};
+static int g_lanes[33][4];
+static bool g_lanes_init = [] {
+    for (int n = 0; n < 33; n++)
+        for (int m = 0; m < 4; m++) g_lanes[n][m] = kLanesGB300[n][m];
+    return true;
+}();
+
+int tuned_lanes(int n, int mode) {
+    const int l = (n >= 1 && n <= 32 && mode >= 0 && mode < 4) ? g_lanes[n][mode] : 0;
+    return l > 0 ? l : default_lanes(n, mode);
+}
 
 int tuned_threads(int n, int mode) {
     const int t = (n >= 1 && n <= 32 && mode >= 0 && mode < 4) ? g_tuned[n][mode] : 0;
@@ -311,6 +362,22 @@ int mi_set_launch_config(int n, int pivot, int threads_per_block) {
 int mi_get_launch_config(int n, int pivot, int* threads_per_block) {
     if (n < 1 || n > 32 || pivot < 0 || pivot > 3) return MI_ERR_INVALID_VALUE;
     if (threads_per_block) *threads_per_block = mi::tuned_threads(n, pivot);
+    return MI_OK;
+}
+
+int mi_set_launch_lanes(int n, int pivot, int lanes_per_matrix) {
+    if (n < 1 || n > 32 || pivot < 0 || pivot > 3 || lanes_per_matrix < 0) return MI_ERR_INVALID_VALUE;
+    const int def = mi::default_lanes(n, pivot), alt = mi::alt_lanes(n, pivot);
+    if (lanes_per_matrix != 0 && lanes_per_matrix != def && (alt == 0 || lanes_per_matrix != alt))
+        return MI_ERR_INVALID_VALUE;
+    mi::g_lanes[n][pivot] = lanes_per_matrix ? lanes_per_matrix : mi::kLanesGB300[n][pivot];
+    return MI_OK;
+}
+
+int mi_get_launch_lanes(int n, int pivot, int* lanes_per_matrix, int* alternative) {
+    if (n < 1 || n > 32 || pivot < 0 || pivot > 3) return MI_ERR_INVALID_VALUE;
+    if (lanes_per_matrix) *lanes_per_matrix = mi::tuned_lanes(n, pivot);
+    if (alternative) *alternative = mi::alt_lanes(n, pivot);
     return MI_OK;
 }
 

@@ -149,6 +149,22 @@ __host__ __device__ constexpr int default_lanes(int n, int mode) {
     return mode == kModePartial ? pow2_at_least(n) : (n > 16 ? 16 : (n > 10 ? 8 : 4));
 }
 
+// The other lanes-per-matrix a size can run at (0: none), chosen per
+// (n, mode) at run time from the tuned table: eight lanes for n = 17..31
+// without partial pivoting -- 8 x 16 register blocks, four matrices per warp,
+// the same bits as sixteen lanes.  Measured on GB300 at 1,000,000 matrices:
+// faster at n = 17..28 in most modes (no pivoting, n = 20: 0.87 against
+// 1.09 ms), slower at n = 29..31 (the reference rule, n = 30: 4.82 against
+// 3.83 ms).
+__host__ __device__ constexpr int alt_lanes(int n, int mode) {
+    return (mode != kModePartial && n > 16 && n < 32) ? 8 : 0;
+}
+
+// Blocks of 256 threads per SM the lane-group kernels are compiled for: two
+// (at most 128 registers), or one for eight lanes above n = 16, whose 8 x 16
+// register blocks need up to 255.
+__host__ __device__ constexpr int lane_min_blocks(int n, int lanes) { return (lanes == 8 && n > 16) ? 1 : 2; }
+
 // ---------------------------------------------------------------------------
 // Geometry per (n, lanes per matrix).
 // ---------------------------------------------------------------------------
@@ -1168,7 +1184,7 @@ struct WarpSmem {
 // block load.
 // ---------------------------------------------------------------------------
 template <int N, int L, int MODE>
-__global__ void __launch_bounds__(256, 2) mi_inverse_kernel(float* __restrict__ A, int32_t* __restrict__ perm_out,
+__global__ void __launch_bounds__(256, lane_min_blocks(N, L)) mi_inverse_kernel(float* __restrict__ A, int32_t* __restrict__ perm_out,
                                                             int32_t* __restrict__ info_out, long long batch,
                                                             int copy_mode, int vec_out,
                                                             const __grid_constant__ CUtensorMap tmap,
@@ -1306,7 +1322,7 @@ __global__ void __launch_bounds__(256, 2) mi_inverse_kernel(float* __restrict__ 
 // go to perm_out[index * 32 ..], info to info_out[index].
 // ---------------------------------------------------------------------------
 template <int N, int L, int MODE>
-__global__ void __launch_bounds__(256, 2) mi_inverse_indexed_kernel(float* __restrict__ base,
+__global__ void __launch_bounds__(256, lane_min_blocks(N, L)) mi_inverse_indexed_kernel(float* __restrict__ base,
                                                                     const long long* __restrict__ offsets,
                                                                     const int* __restrict__ list,
                                                                     const long long* __restrict__ range,

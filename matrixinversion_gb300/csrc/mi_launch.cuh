@@ -121,11 +121,14 @@ cudaError_t launch_wide_gather(float* a, const long long* offsets, const int* li
     return cudaGetLastError();
 }
 
+// Lanes per matrix installed for (n, mode): the tuned table or its run-time
+// override (mi_api.cu, mi_set_launch_lanes); default_lanes when unset.
+int tuned_lanes(int n, int mode);
+
 // The lane-group kernel (mi_inverse_kernel) for a contiguous batch.
-template <int N, int MODE>
+template <int N, int MODE, int L = default_lanes(N, MODE)>
 cudaError_t launch_lanes(float* a, int32_t* perm, int32_t* info, long long batch, int tpb, int grid,
                          cudaStream_t stream) {
-    constexpr int L = default_lanes(N, MODE);
     using G = Geom<N, L>;
     const int warps = tpb / 32;
     const size_t smem = smem_bytes<N, L, MODE>(warps);
@@ -172,6 +175,16 @@ cudaError_t launch_lanes(float* a, int32_t* perm, int32_t* info, long long batch
     return cudaGetLastError();
 }
 
+// The lane-group kernel at the lanes per matrix installed for (n, mode).
+template <int N, int MODE>
+cudaError_t launch_lanes_tuned(float* a, int32_t* perm, int32_t* info, long long batch, int tpb, int grid,
+                               cudaStream_t stream) {
+    constexpr int alt = alt_lanes(N, MODE);
+    if constexpr (alt != 0)
+        if (tuned_lanes(N, MODE) == alt) return launch_lanes<N, MODE, alt>(a, perm, info, batch, tpb, grid, stream);
+    return launch_lanes<N, MODE>(a, perm, info, batch, tpb, grid, stream);
+}
+
 template <int N, int MODE>
 cudaError_t launch(float* a, int32_t* perm, int32_t* info, long long batch, int tpb, int grid,
                    cudaStream_t stream) {
@@ -190,7 +203,7 @@ cudaError_t launch(float* a, int32_t* perm, int32_t* info, long long batch, int 
         if constexpr (MODE == kModePartial && N >= kRowsMin && rows_partial_enabled<N>())
             return launch_rows_partial<N>(a, perm, info, batch, grid, stream);
         else
-            return launch_lanes<N, MODE>(a, perm, info, batch, tpb, grid, stream);
+            return launch_lanes_tuned<N, MODE>(a, perm, info, batch, tpb, grid, stream);
     }
 }
 
@@ -216,7 +229,9 @@ LaunchForm launch_form(long long batch, int tpb) {
         return {kFormRows, RowsGeom<N>::kLanes, RowsGeom<N>::kMats, 32 * kRowsWarps};
     if constexpr (N == WideGeom::N && MODE != kModePartial)
         return {kFormLanes, WideGeom::L, WideGeom::M, tpb < WideGeom::kThreadsMax ? tpb : WideGeom::kThreadsMax};
-    constexpr int L = default_lanes(N, MODE);
+    constexpr int L = default_lanes(N, MODE), alt = alt_lanes(N, MODE);
+    if constexpr (alt != 0)
+        if (tuned_lanes(N, MODE) == alt) return {kFormLanes, alt, Geom<N, alt>::M, tpb};
     return {kFormLanes, L, Geom<N, L>::M, tpb};
 }
 
@@ -226,14 +241,10 @@ LaunchForm launch_form(long long batch, int tpb) {
 using ilaunch_fn = cudaError_t (*)(float*, const long long*, const int*, const long long*, int32_t*, int32_t*, int,
                                    int, cudaStream_t);
 
-template <int N, int MODE>
-cudaError_t launch_indexed(float* base, const long long* offsets, const int* list, const long long* range,
-                           int32_t* perm, int32_t* info, int tpb, int grid, cudaStream_t stream) {
-    if constexpr (N <= tiny_max_indexed<MODE>())
-        return launch_tiny_indexed<N, MODE>(base, offsets, list, range, perm, info, tpb, grid, stream);
-    if constexpr (N == WideGeom::N && MODE != kModePartial)
-        return launch_wide_gather<MODE, true>(base, offsets, list, range, 0, perm, info, tpb, grid, stream);
-    constexpr int L = default_lanes(N, MODE);
+// The lane-group kernel of a descriptor bucket at L lanes per matrix.
+template <int N, int MODE, int L>
+cudaError_t launch_indexed_lanes(float* base, const long long* offsets, const int* list, const long long* range,
+                                 int32_t* perm, int32_t* info, int tpb, int grid, cudaStream_t stream) {
     const int warps = tpb / 32;
     const size_t smem = smem_bytes<N, L, MODE>(warps);
     auto kern = mi_inverse_indexed_kernel<N, L, MODE>;
@@ -254,6 +265,22 @@ cudaError_t launch_indexed(float* base, const long long* offsets, const int* lis
     }
     kern<<<grid, tpb, smem, stream>>>(base, offsets, list, range, perm, info);
     return cudaGetLastError();
+}
+
+template <int N, int MODE>
+cudaError_t launch_indexed(float* base, const long long* offsets, const int* list, const long long* range,
+                           int32_t* perm, int32_t* info, int tpb, int grid, cudaStream_t stream) {
+    if constexpr (N <= tiny_max_indexed<MODE>())
+        return launch_tiny_indexed<N, MODE>(base, offsets, list, range, perm, info, tpb, grid, stream);
+    if constexpr (N == WideGeom::N && MODE != kModePartial)
+        return launch_wide_gather<MODE, true>(base, offsets, list, range, 0, perm, info, tpb, grid, stream);
+    // the lanes per matrix of the contiguous call (either gives the same bits)
+    constexpr int alt = alt_lanes(N, MODE);
+    if constexpr (alt != 0)
+        if (tuned_lanes(N, MODE) == alt)
+            return launch_indexed_lanes<N, MODE, alt>(base, offsets, list, range, perm, info, tpb, grid, stream);
+    return launch_indexed_lanes<N, MODE, default_lanes(N, MODE)>(base, offsets, list, range, perm, info, tpb, grid,
+                                                                 stream);
 }
 
 extern const ilaunch_fn kITableNone[33];

@@ -1,6 +1,8 @@
 """Launch-configuration table (CPU: the table itself) and the autotuner (GPU)."""
 import json
 
+import numpy as np
+
 import pytest
 
 from matrixinversion_gb300 import _lib, autotune
@@ -58,9 +60,12 @@ def test_tuning_installs_best_and_keeps_results(mi_gpu, oracle):
     assert autotune.get_config(8, "reference") == shipped8
     best = table[(20, "reference")]["best"]
     assert best in (64, 256) and autotune.get_config(20, "reference") == best
+    assert table[(20, "reference")]["lanes"] in (8, 16)            # n = 20 runs at either width
+    assert set(table[(20, "reference")]["ms_by_lanes"]) == {8, 16}
     X, _, _ = mi_gpu.batched_inverse(A, "reference")
     assert torch.equal(X, ref)
     autotune.set_config(20, "reference", 0)
+    autotune.set_lanes(20, "reference", 0)
 
 
 def test_fixed_block_sizes_are_reported_not_timed(lib):
@@ -72,3 +77,72 @@ def test_fixed_block_sizes_are_reported_not_timed(lib):
     table = autotune.tune([16], ["partial"], batch=4096)
     assert table == {(16, "partial"): {"best": 0, "ms": {}, "form": "rows"}}
     assert {(n, m): autotune.get_config(n, m) for n in (1, 8, 16) for m in ("none", "reference", "partial")} == before
+
+
+def test_lanes_per_matrix_knob(lib, tmp_path):
+    """Sizes 17..31 without partial pivoting run at 16 or 8 lanes per matrix,
+    every other (n, mode) at one width; the entry installs, restores, and
+    round-trips through a saved table; mi_query_launch reports it."""
+    import matrixinversion_gb300 as mi
+
+    shipped, alt = autotune.get_lanes(24, "reference")
+    assert alt == 8 and shipped in (8, 16)
+    for lanes in (8, 16):
+        autotune.set_lanes(24, "reference", lanes)
+        assert autotune.get_lanes(24, "reference") == (lanes, 8)
+        assert mi.query_launch(24, "reference", 10**6)["lanes_per_matrix"] == lanes
+    autotune.set_lanes(24, "reference", 0)
+    assert autotune.get_lanes(24, "reference") == (shipped, 8)
+    assert autotune.get_lanes(12, "reference") == (8, 0)          # one width
+    assert autotune.get_lanes(24, "partial")[1] == 0
+    assert autotune.get_lanes(32, "reference")[1] == 0
+    for bad in ((24, "reference", 4), (24, "reference", 32), (12, "reference", 16), (24, "partial", 8),
+                (0, "none", 8), (33, "none", 8)):
+        with pytest.raises(_lib.MatrixInversionError):
+            autotune.set_lanes(*bad)
+    table = {(24, "none"): {"best": 128, "ms": {128: 0.5}, "lanes": 8,
+                            "ms_by_lanes": {8: {128: 0.5}, 16: {128: 0.6}}}}
+    path = str(tmp_path / "t.json")
+    autotune.save(table, path)
+    assert autotune.load(path) == table
+    assert autotune.get_lanes(24, "none")[0] == 8 and autotune.get_config(24, "none") == 128
+    autotune.set_lanes(24, "none", 0)
+    autotune.set_config(24, "none", 0)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n", [17, 24, 29, 31])
+def test_both_widths_give_the_same_bits(mi_gpu, oracle, n):
+    """16 and 8 lanes per matrix run the same arithmetic per element: the same
+    inverse, pivots and info in every non-partial mode, for a contiguous call
+    and for a descriptor bucket."""
+    import torch
+
+    from matrixinversion_gb300 import descr
+
+    A = oracle.uniform(700 + n, 1500, n)
+    A[7] = 0.0                                                     # singular: info set
+    for mode in ("none", "reference", "reference_serial"):
+        M = A + np.float32(n) * np.eye(n, dtype=np.float32) if mode == "none" else A
+        out = {}
+        for lanes in (16, 8):
+            autotune.set_lanes(n, mode, lanes)
+            X, P, I = mi_gpu.batched_inverse(torch.from_numpy(M).cuda(), mode)
+            packed, offsets, ns = descr.pack(list(M))
+            d = torch.from_numpy(packed).cuda()
+            perm = torch.empty((len(M), 32), dtype=torch.int32, device="cuda")
+            info = torch.empty((len(M),), dtype=torch.int32, device="cuda")
+            flags = torch.full((len(M),), _lib.PIVOT_MODES[mode], dtype=torch.int32, device="cuda")
+            descr.batched_inverse_descr_(d, torch.from_numpy(offsets).cuda(), torch.from_numpy(ns).cuda(), flags,
+                                         perm=perm, info=info)
+            torch.cuda.synchronize()
+            out[lanes] = (X.cpu().numpy(), P.cpu().numpy(), I.cpu().numpy(), descr.unpack(d.cpu().numpy(), offsets, ns),
+                          perm.cpu().numpy()[:, :n], info.cpu().numpy())
+        autotune.set_lanes(n, mode, 0)
+        x16, p16, i16, g16, q16, j16 = out[16]
+        x8, p8, i8, g8, q8, j8 = out[8]
+        assert np.array_equal(x16.view(np.int32), x8.view(np.int32)), (n, mode)
+        assert np.array_equal(p16, p8) and np.array_equal(i16, i8)
+        assert all(np.array_equal(a.view(np.int32), b.view(np.int32)) for a, b in zip(g16, g8))
+        assert all(np.array_equal(a.view(np.int32), x16[i].view(np.int32)) for i, a in enumerate(g16))
+        assert np.array_equal(q16, q8) and np.array_equal(q16, p16) and np.array_equal(j16, i16)
