@@ -317,11 +317,13 @@ int mi_get_launch_config(int n, int pivot, int* threads_per_block);
  * the choice measured on GB300; every other (n, pivot) has one width.  Set
  * lanes_per_matrix to that width, the alternative, or 0 to restore the table's
  * entry; anything else -> MI_ERR_INVALID_VALUE.  mi_get_launch_lanes returns
- * the installed width and the alternative (0 if none).  Contiguous calls and
- * descriptor buckets both follow the entry.
+ * the installed width and the other width the size can run at (0 if none).
+ * Contiguous calls of at least MI_LANES_ALT_MIN_BATCH matrices follow the
+ * entry; smaller ones and descriptor buckets run at the default width.
  */
+#define MI_LANES_ALT_MIN_BATCH 131072
 int mi_set_launch_lanes(int n, int pivot, int lanes_per_matrix);
-int mi_get_launch_lanes(int n, int pivot, int* lanes_per_matrix, int* alternative);
+int mi_get_launch_lanes(int n, int pivot, int* lanes_per_matrix, int* other);
 
 const char* mi_error_string(int status);
 /* Text of the last CUDA error seen by this thread ("" if none). */

@@ -17,6 +17,7 @@ MI_ERR_MISALIGNED = -3
 MI_ERR_CUDA = -4
 MI_ERR_SCRATCH_LIMIT = -5
 MI_NOALLOC_MAX_COUNT = 262144
+MI_LANES_ALT_MIN_BATCH = 131072      # contiguous batches from this size follow the tuned lanes per matrix
 
 # flags of mi_device_error
 MI_DEVERR_COPY_TIMEOUT, MI_DEVERR_MMA_TIMEOUT = 1, 2

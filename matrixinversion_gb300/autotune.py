@@ -74,8 +74,9 @@ def tune(ns=range(1, 33), modes=("none", "reference"), batch: int = 262144, iter
         work = torch.empty_like(src)
         for mode in tunable:
             s = src + n * torch.eye(n, device="cuda") if mode == "none" else src
-            installed, alt = get_lanes(n, mode)
-            widths = [installed] + ([alt] if alt and alt != installed else [])
+            installed, other = get_lanes(n, mode)
+            # below MI_LANES_ALT_MIN_BATCH every call runs at the default width
+            widths = [installed] + ([other] if other and batch >= _lib.MI_LANES_ALT_MIN_BATCH else [])
             by_lanes = {}
             for lanes in widths:
                 if len(widths) > 1:
@@ -110,7 +111,7 @@ def set_lanes(n: int, mode: str, lanes_per_matrix: int) -> None:
 
 
 def get_lanes(n: int, mode: str) -> tuple[int, int]:
-    """(installed lanes per matrix, the alternative width or 0)."""
+    """(installed lanes per matrix, the other width the size can run at, or 0)."""
     v, alt = ctypes.c_int(0), ctypes.c_int(0)
     _lib.check(_lib.load().mi_get_launch_lanes(int(n), _lib.PIVOT_MODES[mode], ctypes.byref(v), ctypes.byref(alt)))
     return v.value, alt.value

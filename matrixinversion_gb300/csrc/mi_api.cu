@@ -374,10 +374,11 @@ int mi_set_launch_lanes(int n, int pivot, int lanes_per_matrix) {
     return MI_OK;
 }
 
-int mi_get_launch_lanes(int n, int pivot, int* lanes_per_matrix, int* alternative) {
+int mi_get_launch_lanes(int n, int pivot, int* lanes_per_matrix, int* other) {
     if (n < 1 || n > 32 || pivot < 0 || pivot > 3) return MI_ERR_INVALID_VALUE;
-    if (lanes_per_matrix) *lanes_per_matrix = mi::tuned_lanes(n, pivot);
-    if (alternative) *alternative = mi::alt_lanes(n, pivot);
+    const int installed = mi::tuned_lanes(n, pivot), alt = mi::alt_lanes(n, pivot);
+    if (lanes_per_matrix) *lanes_per_matrix = installed;
+    if (other) *other = alt == 0 ? 0 : (installed == alt ? mi::default_lanes(n, pivot) : alt);
     return MI_OK;
 }
 

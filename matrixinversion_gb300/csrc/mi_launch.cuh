@@ -9,6 +9,7 @@
 #include <cstdint>
 #include <cstring>
 
+#include "mi_inverse.h"
 #include "mi_kernel.cuh"
 
 namespace mi {
@@ -175,13 +176,18 @@ cudaError_t launch_lanes(float* a, int32_t* perm, int32_t* info, long long batch
     return cudaGetLastError();
 }
 
-// The lane-group kernel at the lanes per matrix installed for (n, mode).
+// The lane-group kernel at the lanes per matrix installed for (n, mode) --
+// from MI_LANES_ALT_MIN_BATCH matrices up; smaller batches run at the
+// default width (measured on GB300: eight lanes, one block of eight warps per
+// SM, win on batches of 262,144 and 1,000,000 matrices and lose on batches of
+// about 16,000, where sixteen warps per SM hide more of each step's latency).
 template <int N, int MODE>
 cudaError_t launch_lanes_tuned(float* a, int32_t* perm, int32_t* info, long long batch, int tpb, int grid,
                                cudaStream_t stream) {
     constexpr int alt = alt_lanes(N, MODE);
     if constexpr (alt != 0)
-        if (tuned_lanes(N, MODE) == alt) return launch_lanes<N, MODE, alt>(a, perm, info, batch, tpb, grid, stream);
+        if (batch >= MI_LANES_ALT_MIN_BATCH && tuned_lanes(N, MODE) == alt)
+            return launch_lanes<N, MODE, alt>(a, perm, info, batch, tpb, grid, stream);
     return launch_lanes<N, MODE>(a, perm, info, batch, tpb, grid, stream);
 }
 
@@ -231,7 +237,8 @@ LaunchForm launch_form(long long batch, int tpb) {
         return {kFormLanes, WideGeom::L, WideGeom::M, tpb < WideGeom::kThreadsMax ? tpb : WideGeom::kThreadsMax};
     constexpr int L = default_lanes(N, MODE), alt = alt_lanes(N, MODE);
     if constexpr (alt != 0)
-        if (tuned_lanes(N, MODE) == alt) return {kFormLanes, alt, Geom<N, alt>::M, tpb};
+        if (batch >= MI_LANES_ALT_MIN_BATCH && tuned_lanes(N, MODE) == alt)
+            return {kFormLanes, alt, Geom<N, alt>::M, tpb};
     return {kFormLanes, L, Geom<N, L>::M, tpb};
 }
 
@@ -274,11 +281,9 @@ cudaError_t launch_indexed(float* base, const long long* offsets, const int* lis
         return launch_tiny_indexed<N, MODE>(base, offsets, list, range, perm, info, tpb, grid, stream);
     if constexpr (N == WideGeom::N && MODE != kModePartial)
         return launch_wide_gather<MODE, true>(base, offsets, list, range, 0, perm, info, tpb, grid, stream);
-    // the lanes per matrix of the contiguous call (either gives the same bits)
-    constexpr int alt = alt_lanes(N, MODE);
-    if constexpr (alt != 0)
-        if (tuned_lanes(N, MODE) == alt)
-            return launch_indexed_lanes<N, MODE, alt>(base, offsets, list, range, perm, info, tpb, grid, stream);
+    // the default width: a bucket's size is known only on the device, and
+    // buckets are typically below MI_LANES_ALT_MIN_BATCH (either width gives
+    // the same bits)
     return launch_indexed_lanes<N, MODE, default_lanes(N, MODE)>(base, offsets, list, range, perm, info, tpb, grid,
                                                                  stream);
 }

@@ -60,8 +60,9 @@ def test_tuning_installs_best_and_keeps_results(mi_gpu, oracle):
     assert autotune.get_config(8, "reference") == shipped8
     best = table[(20, "reference")]["best"]
     assert best in (64, 256) and autotune.get_config(20, "reference") == best
-    assert table[(20, "reference")]["lanes"] in (8, 16)            # n = 20 runs at either width
-    assert set(table[(20, "reference")]["ms_by_lanes"]) == {8, 16}
+    # below MI_LANES_ALT_MIN_BATCH every call runs at the default width, so
+    # the tuner compares widths only from that batch up
+    assert "lanes" not in table[(20, "reference")]
     X, _, _ = mi_gpu.batched_inverse(A, "reference")
     assert torch.equal(X, ref)
     autotune.set_config(20, "reference", 0)
@@ -85,14 +86,14 @@ def test_lanes_per_matrix_knob(lib, tmp_path):
     round-trips through a saved table; mi_query_launch reports it."""
     import matrixinversion_gb300 as mi
 
-    shipped, alt = autotune.get_lanes(24, "reference")
-    assert alt == 8 and shipped in (8, 16)
+    shipped, other = autotune.get_lanes(24, "reference")
+    assert {shipped, other} == {8, 16}
     for lanes in (8, 16):
         autotune.set_lanes(24, "reference", lanes)
-        assert autotune.get_lanes(24, "reference") == (lanes, 8)
+        assert autotune.get_lanes(24, "reference") == (lanes, 24 - lanes)
         assert mi.query_launch(24, "reference", 10**6)["lanes_per_matrix"] == lanes
     autotune.set_lanes(24, "reference", 0)
-    assert autotune.get_lanes(24, "reference") == (shipped, 8)
+    assert autotune.get_lanes(24, "reference") == (shipped, other)
     assert autotune.get_lanes(12, "reference") == (8, 0)          # one width
     assert autotune.get_lanes(24, "partial")[1] == 0
     assert autotune.get_lanes(32, "reference")[1] == 0
@@ -113,36 +114,60 @@ def test_lanes_per_matrix_knob(lib, tmp_path):
 @pytest.mark.gpu
 @pytest.mark.parametrize("n", [17, 24, 29, 31])
 def test_both_widths_give_the_same_bits(mi_gpu, oracle, n):
-    """16 and 8 lanes per matrix run the same arithmetic per element: the same
-    inverse, pivots and info in every non-partial mode, for a contiguous call
-    and for a descriptor bucket."""
+    """16 and 8 lanes per matrix run the same arithmetic per element: a
+    contiguous batch large enough to follow the entry (MI_LANES_ALT_MIN_BATCH
+    matrices) gives the same inverse, pivots and info at either width in every
+    non-partial mode, and so does a descriptor bucket of its first matrices
+    (which runs at the default width); a smaller batch runs at the default
+    width whatever the entry."""
     import torch
 
+    import matrixinversion_gb300 as mi
     from matrixinversion_gb300 import descr
 
-    A = oracle.uniform(700 + n, 1500, n)
+    big = _lib.MI_LANES_ALT_MIN_BATCH
+    g = torch.Generator(device="cuda").manual_seed(700 + n)
+    A = torch.rand(big, n, n, generator=g, device="cuda") * 2 - 1
     A[7] = 0.0                                                     # singular: info set
     for mode in ("none", "reference", "reference_serial"):
-        M = A + np.float32(n) * np.eye(n, dtype=np.float32) if mode == "none" else A
+        M = A + n * torch.eye(n, device="cuda") if mode == "none" else A
         out = {}
         for lanes in (16, 8):
             autotune.set_lanes(n, mode, lanes)
-            X, P, I = mi_gpu.batched_inverse(torch.from_numpy(M).cuda(), mode)
-            packed, offsets, ns = descr.pack(list(M))
-            d = torch.from_numpy(packed).cuda()
-            perm = torch.empty((len(M), 32), dtype=torch.int32, device="cuda")
-            info = torch.empty((len(M),), dtype=torch.int32, device="cuda")
-            flags = torch.full((len(M),), _lib.PIVOT_MODES[mode], dtype=torch.int32, device="cuda")
-            descr.batched_inverse_descr_(d, torch.from_numpy(offsets).cuda(), torch.from_numpy(ns).cuda(), flags,
-                                         perm=perm, info=info)
-            torch.cuda.synchronize()
-            out[lanes] = (X.cpu().numpy(), P.cpu().numpy(), I.cpu().numpy(), descr.unpack(d.cpu().numpy(), offsets, ns),
-                          perm.cpu().numpy()[:, :n], info.cpu().numpy())
+            assert mi.query_launch(n, mode, big)["lanes_per_matrix"] == lanes
+            assert mi.query_launch(n, mode, big - 1)["lanes_per_matrix"] == 16
+            X, P, I = mi_gpu.batched_inverse(M, mode)
+            out[lanes] = (X, P, I)
         autotune.set_lanes(n, mode, 0)
-        x16, p16, i16, g16, q16, j16 = out[16]
-        x8, p8, i8, g8, q8, j8 = out[8]
-        assert np.array_equal(x16.view(np.int32), x8.view(np.int32)), (n, mode)
-        assert np.array_equal(p16, p8) and np.array_equal(i16, i8)
-        assert all(np.array_equal(a.view(np.int32), b.view(np.int32)) for a, b in zip(g16, g8))
-        assert all(np.array_equal(a.view(np.int32), x16[i].view(np.int32)) for i, a in enumerate(g16))
-        assert np.array_equal(q16, q8) and np.array_equal(q16, p16) and np.array_equal(j16, i16)
+        (x16, p16, i16), (x8, p8, i8) = out[16], out[8]
+        assert torch.equal(x16.view(torch.int32), x8.view(torch.int32)), (n, mode)
+        assert torch.equal(p16, p8) and torch.equal(i16, i8)
+        assert (int(i8[7]) != 0) == (mode != "none")             # + n I makes it regular without pivoting
+        # a descriptor bucket of the first 300 matrices: the same bits
+        head = [m for m in M[:300].cpu().numpy()]
+        packed, offsets, ns = descr.pack(head)
+        d = torch.from_numpy(packed).cuda()
+        perm = torch.empty((len(head), 32), dtype=torch.int32, device="cuda")
+        flags = torch.full((len(head),), _lib.PIVOT_MODES[mode], dtype=torch.int32, device="cuda")
+        descr.batched_inverse_descr_(d, torch.from_numpy(offsets).cuda(), torch.from_numpy(ns).cuda(), flags,
+                                     perm=perm)
+        got = descr.unpack(d.cpu().numpy(), offsets, ns)
+        x8h = x8[:300].cpu().numpy()
+        assert all(np.array_equal(a.view(np.int32), x8h[i].view(np.int32)) for i, a in enumerate(got))
+        assert np.array_equal(perm.cpu().numpy()[:, :n], p8[:300].cpu().numpy())
+
+
+@pytest.mark.gpu
+def test_tuning_compares_widths_from_the_batch_threshold(mi_gpu):
+    """At MI_LANES_ALT_MIN_BATCH matrices the tuner times both widths of a
+    size that has two and installs the faster, leaving the results unchanged."""
+    import torch
+
+    shipped = autotune.get_lanes(25, "none")[0]
+    table = autotune.tune([25], ["none"], batch=_lib.MI_LANES_ALT_MIN_BATCH, iters=1, candidates=(256,))
+    e = table[(25, "none")]
+    assert e["lanes"] in (8, 16) and set(e["ms_by_lanes"]) == {8, 16}
+    assert autotune.get_lanes(25, "none")[0] == e["lanes"]
+    autotune.set_lanes(25, "none", 0)
+    autotune.set_config(25, "none", 0)
+    assert autotune.get_lanes(25, "none")[0] == shipped
