@@ -9,16 +9,21 @@
 //   * admission: first come, first served; an arrived request is admitted
 //     when the device pool (the HBM budget, carved once by the caller) has a
 //     free extent for it (ExtentPool, first fit), and its host-to-device copy
-//     goes out at once on the copy stream;
+//     goes out at once on the copy stream -- one copy for a run of requests
+//     admitted together that follow each other both in the host ring and in
+//     the pool;
 //   * batching: whenever fewer than two batches are computing, every admitted
 //     request not yet computed goes into one launch -- one descriptor call
 //     over the pool (its matrices' offsets into the pool staged through a
 //     pinned table), or one contiguous call for a batch of a single request;
-//   * completion, per request: its results are copied back to its place in
-//     the host ring on the copy-out stream with an event of its own; when the
-//     loop sees that event it records the request's completion time and frees
-//     its extent, so a request's latency does not wait for the rest of its
-//     batch to leave and its memory serves the next arrivals at once.
+//   * completion: results are copied back to their place in the host ring
+//     on the copy-out stream, one copy (with an event of its own) per run of
+//     a batch's requests that follow each other in the pool and in the ring;
+//     when the loop sees that event it records those requests' completion
+//     time and frees their extents, so a request's latency does not wait for
+//     the rest of its batch to leave and its memory serves the next arrivals
+//     at once.  (One copy per request made the loop issue-bound with host
+//     copies.)
 //
 // With requests already in device memory (d_ring != NULL: an upstream device
 // stage wrote them there; the caller counts that memory against its budget)
@@ -127,7 +132,12 @@ int mi_serve_run(int64_t num_requests, const double* arrival_s, const int64_t* k
     std::vector<int64_t> ext(num_requests, -1);            // pool extent of each admitted request
     std::vector<double> done(num_requests, -1.0);
     std::deque<Batch> computing;
-    std::deque<std::pair<int64_t, cudaEvent_t>> leaving;    // results on their way to the host ring
+    // results on their way to the host ring: requests [first, last) of one copy
+    struct Leaving {
+        int64_t first, last;
+        cudaEvent_t home;
+    };
+    std::deque<Leaving> leaving;
     int64_t admitted = 0, launched = 0, completed = 0, batches = 0, tables_used = 0;
 
     const auto t0 = std::chrono::steady_clock::now();
@@ -140,15 +150,16 @@ int mi_serve_run(int64_t num_requests, const double* arrival_s, const int64_t* k
         bool idle = true;
         // ---- completions: results home (per request), batches finished
         while (!leaving.empty()) {
-            const cudaError_t q = cudaEventQuery(leaving.front().second);
+            const cudaError_t q = cudaEventQuery(leaving.front().home);
             if (q == cudaErrorNotReady) break;
             if (q != cudaSuccess) return fail(q, "serving: result copy");
-            const int64_t r = leaving.front().first;
-            done[r] = t;
-            pool.release(ext[r], len[r]);
-            res.spare.push_back(leaving.front().second);
+            for (int64_t r = leaving.front().first; r < leaving.front().last; r++) {
+                done[r] = t;
+                pool.release(ext[r], len[r]);
+                completed++;
+            }
+            res.spare.push_back(leaving.front().home);
             leaving.pop_front();
-            completed++;
             idle = false;
         }
         while (!computing.empty()) {
@@ -163,22 +174,37 @@ int mi_serve_run(int64_t num_requests, const double* arrival_s, const int64_t* k
             computing.pop_front();
             idle = false;
         }
-        // ---- admission: arrived requests, first come first served, as extents free
+        // ---- admission: arrived requests, first come first served, as extents free.
+        // Requests that follow each other both in the host ring and in the pool
+        // (offset + padded length = the next offset, on both sides) go in by one
+        // copy; the padding it carries lies inside the ring and the extent.
+        int64_t run = -1;                                    // first request of the pending copy
+        auto flush_in = [&](int64_t end) -> cudaError_t {   // copy requests [run, end)
+            if (run < 0 || end <= run) return cudaSuccess;
+            const int64_t last = end - 1;
+            const int64_t floats = ring_off[last] - ring_off[run] + k[last] * n[last] * n[last];
+            return cudaMemcpyAsync(d_pool + ext[run], h_in + ring_off[run], (size_t)floats * sizeof(float),
+                                   cudaMemcpyHostToDevice, res.h2d);
+        };
         while (admitted < num_requests && arrival_s[admitted] <= t) {
             if (!resident) {
                 const int64_t off = pool.alloc(len[admitted]);
                 if (off < 0) break;                          // wait for memory, keep the order
                 ext[admitted] = off;
-                e = cudaMemcpyAsync(d_pool + off, h_in + ring_off[admitted],
-                                    (size_t)(k[admitted] * n[admitted] * n[admitted]) * sizeof(float),
-                                    cudaMemcpyHostToDevice, res.h2d);
-                if (e != cudaSuccess) return fail(e, "serving: request copy");
+                const int64_t prev = admitted - 1;
+                const bool joins = run >= 0 && ring_off[admitted] == ring_off[prev] + len[prev] &&
+                                   off == ext[prev] + len[prev];
+                if (!joins) {
+                    if ((e = flush_in(admitted)) != cudaSuccess) return fail(e, "serving: request copy");
+                    run = admitted;
+                }
             } else {
                 ext[admitted] = ring_off[admitted];
             }
             admitted++;
             idle = false;
         }
+        if ((e = flush_in(admitted)) != cudaSuccess) return fail(e, "serving: request copy");
         // ---- batching: every admitted request not yet computed, into one launch
         if (launched < admitted && (int)computing.size() < kInFlight) {
             int64_t last = launched, mats = 0;
@@ -228,14 +254,22 @@ int mi_serve_run(int64_t num_requests, const double* arrival_s, const int64_t* k
                 return fail(e, "serving: batch event");
             if (!resident) {
                 if ((e = cudaStreamWaitEvent(res.d2h, b.done, 0)) != cudaSuccess) return fail(e, "serving: results");
-                for (int64_t r = launched; r < last; r++) {
+                // results out by one copy per run of requests that follow each
+                // other in the pool and in the ring; each run completes at its
+                // copy's event
+                for (int64_t r0 = launched; r0 < last;) {
+                    int64_t r1 = r0 + 1;
+                    while (r1 < last && ring_off[r1] == ring_off[r1 - 1] + len[r1 - 1] &&
+                           ext[r1] == ext[r1 - 1] + len[r1 - 1])
+                        r1++;
+                    const int64_t floats = ring_off[r1 - 1] - ring_off[r0] + k[r1 - 1] * n[r1 - 1] * n[r1 - 1];
                     cudaEvent_t home = nullptr;
-                    if ((e = cudaMemcpyAsync(h_out + ring_off[r], d_pool + ext[r],
-                                             (size_t)(k[r] * n[r] * n[r]) * sizeof(float), cudaMemcpyDeviceToHost,
-                                             res.d2h)) != cudaSuccess ||
+                    if ((e = cudaMemcpyAsync(h_out + ring_off[r0], d_pool + ext[r0], (size_t)floats * sizeof(float),
+                                             cudaMemcpyDeviceToHost, res.d2h)) != cudaSuccess ||
                         (e = res.event(&home)) != cudaSuccess || (e = cudaEventRecord(home, res.d2h)) != cudaSuccess)
                         return fail(e, "serving: result copy");
-                    leaving.emplace_back(r, home);
+                    leaving.push_back({r0, r1, home});
+                    r0 = r1;
                 }
             }
             computing.push_back(b);
