@@ -129,6 +129,7 @@ int mi_serve_run(int64_t num_requests, const double* arrival_s, const int64_t* k
     const int64_t base_floats = resident ? INT64_MAX / 2 : pool_floats;
 
     mi::ExtentPool pool(resident ? 0 : pool_floats);
+    constexpr int64_t kRunFloats = int64_t(1) << 24;       // the longest copy in: 64 MB
     std::vector<int64_t> ext(num_requests, -1);            // pool extent of each admitted request
     std::vector<double> done(num_requests, -1.0);
     std::deque<Batch> computing;
@@ -138,6 +139,8 @@ int mi_serve_run(int64_t num_requests, const double* arrival_s, const int64_t* k
         cudaEvent_t home;
     };
     std::deque<Leaving> leaving;
+    // inputs on their way in: requests before `end` are on the device once the event has fired
+    std::deque<std::pair<int64_t, cudaEvent_t>> arriving;
     int64_t admitted = 0, launched = 0, completed = 0, batches = 0, tables_used = 0;
 
     const auto t0 = std::chrono::steady_clock::now();
@@ -178,13 +181,21 @@ int mi_serve_run(int64_t num_requests, const double* arrival_s, const int64_t* k
         // Requests that follow each other both in the host ring and in the pool
         // (offset + padded length = the next offset, on both sides) go in by one
         // copy; the padding it carries lies inside the ring and the extent.
+        // A copy covers at most kRunFloats (64 MB) and records an event, so a
+        // batch waits only for the copies of its own requests.
         int64_t run = -1;                                    // first request of the pending copy
         auto flush_in = [&](int64_t end) -> cudaError_t {   // copy requests [run, end)
             if (run < 0 || end <= run) return cudaSuccess;
             const int64_t last = end - 1;
             const int64_t floats = ring_off[last] - ring_off[run] + k[last] * n[last] * n[last];
-            return cudaMemcpyAsync(d_pool + ext[run], h_in + ring_off[run], (size_t)floats * sizeof(float),
-                                   cudaMemcpyHostToDevice, res.h2d);
+            cudaError_t err = cudaMemcpyAsync(d_pool + ext[run], h_in + ring_off[run], (size_t)floats * sizeof(float),
+                                              cudaMemcpyHostToDevice, res.h2d);
+            cudaEvent_t in = nullptr;
+            if (err == cudaSuccess) err = res.event(&in);
+            if (err == cudaSuccess) err = cudaEventRecord(in, res.h2d);
+            if (err == cudaSuccess) arriving.emplace_back(end, in);
+            run = -1;
+            return err;
         };
         while (admitted < num_requests && arrival_s[admitted] <= t) {
             if (!resident) {
@@ -193,7 +204,9 @@ int mi_serve_run(int64_t num_requests, const double* arrival_s, const int64_t* k
                 ext[admitted] = off;
                 const int64_t prev = admitted - 1;
                 const bool joins = run >= 0 && ring_off[admitted] == ring_off[prev] + len[prev] &&
-                                   off == ext[prev] + len[prev];
+                                   off == ext[prev] + len[prev] &&
+                                   ring_off[admitted] + k[admitted] * n[admitted] * n[admitted] - ring_off[run] <=
+                                       kRunFloats;
                 if (!joins) {
                     if ((e = flush_in(admitted)) != cudaSuccess) return fail(e, "serving: request copy");
                     run = admitted;
@@ -214,12 +227,19 @@ int mi_serve_run(int64_t num_requests, const double* arrival_s, const int64_t* k
                 n_mask |= 1u << (n[last] - 1);
                 last++;
             }
-            cudaEvent_t ready = nullptr;
             if (!resident) {
-                if ((e = res.event(&ready)) != cudaSuccess || (e = cudaEventRecord(ready, res.h2d)) != cudaSuccess ||
-                    (e = cudaStreamWaitEvent(res.cmp, ready, 0)) != cudaSuccess)
+                // the copy that brings in the batch's last request (the copies
+                // before it precede it on the copy stream); copies that end at
+                // or before this batch's end are not needed by later batches
+                auto it = arriving.begin();
+                while (it != arriving.end() && it->first < last) ++it;
+                if (it == arriving.end()) return fail(cudaErrorUnknown, "serving: batch inputs");
+                if ((e = cudaStreamWaitEvent(res.cmp, it->second, 0)) != cudaSuccess)
                     return fail(e, "serving: batch inputs");
-                res.spare.push_back(ready);   // recorded and waited on: free for reuse in stream order
+                while (!arriving.empty() && arriving.front().first <= last) {
+                    res.spare.push_back(arriving.front().second);   // waited on in stream order: free for reuse
+                    arriving.pop_front();
+                }
             }
             int status = MI_OK;
             if (last - launched == 1) {
