@@ -132,15 +132,29 @@ int mi_query_launch(int n, int pivot, int64_t batch, int threads_per_block, int*
  * or a matrix that is not inside d_packed; not processed, not touched).
  * n_mask: bit n-1 set if size n may occur (0 = all sizes); mode_mask: bit m
  * set if pivot mode m may occur (0 = all) -- buckets outside the masks are
- * not launched.  d_workspace: caller-owned device scratch of at least
+ * not processed.  d_workspace: caller-owned device scratch of at least
  * mi_descr_workspace_bytes(count) bytes, 256-byte aligned.  The call issues
  * only stream-ordered work (no host synchronisation), so it can be captured
- * into a CUDA graph.
+ * into a CUDA graph: a memset and three bucketing kernels (count, scan,
+ * scatter), then either one persistent launch per (n, mode) bucket inside the
+ * masks (the default) or, after mi_set_descr_chunk(c > 0), ONE persistent
+ * launch whose warps take chunks of about c input floats (at most 8 groups)
+ * from a device counter, largest n first, for every bucket (the runtime-n
+ * counterpart of no_templ/luBatchedInplace.cuh:82-131).  Every matrix gets
+ * the bits of the contiguous call either way.
  */
 int mi_inverse_descr_f32(float* d_packed, int64_t packed_floats, const int64_t* d_offsets, const int32_t* d_n,
                          const int32_t* d_flags, int32_t* d_perm, int32_t* d_info, int64_t count, uint32_t n_mask,
                          uint32_t mode_mask, void* d_workspace, size_t workspace_bytes, void* stream);
 size_t mi_descr_workspace_bytes(int64_t count);
+/*
+ * Form of mi_inverse_descr_f32: 0 (the default) = one launch per (n, mode)
+ * bucket; c > 0 = the single persistent launch with chunks of about c input
+ * floats (1 to 8 groups of matrices each).  Process-wide; the same bits
+ * either way.  MI_ERR_INVALID_VALUE for a negative size.
+ */
+int mi_set_descr_chunk(int chunk_floats);
+int mi_get_descr_chunk(void);
 
 /*
  * mi_inverse_descr_f32 without a caller workspace -- no counterpart in the

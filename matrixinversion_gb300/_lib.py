@@ -108,6 +108,10 @@ def load(path: str | None = None):
     L.mi_set_launch_lanes.restype = i32
     L.mi_get_launch_lanes.argtypes = [i32, i32, ip, ip]
     L.mi_get_launch_lanes.restype = i32
+    L.mi_set_descr_chunk.argtypes = [i32]
+    L.mi_set_descr_chunk.restype = i32
+    L.mi_get_descr_chunk.argtypes = []
+    L.mi_get_descr_chunk.restype = i32
     _lib = L
     return L
 
@@ -145,6 +149,8 @@ def exported_symbols() -> list[str]:
         "mi_get_launch_config",
         "mi_set_launch_lanes",
         "mi_get_launch_lanes",
+        "mi_set_descr_chunk",
+        "mi_get_descr_chunk",
         "mi_set_wait_test",
         "mi_serve_scratch_bytes",
         "mi_serve_run",

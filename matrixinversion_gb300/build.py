@@ -1,8 +1,11 @@
 """In-tree build of the CUDA library ``lib/libmi_inverse.so`` for sm_103a.
 
 Each translation unit under ``csrc/`` is compiled by its own nvcc process (in
-parallel), then linked with ``nvcc -shared``.  Objects are rebuilt only when a
-source or header is newer than the object.
+parallel), then linked with ``nvcc -shared``.  The units of the single
+persistent descriptor launch (RDC_UNITS: the kernel and its 128 walks, one
+unit per pivot mode) are relocatable device code, joined by one device-link
+step before the library link.  Objects are rebuilt only when a source or
+header is newer than the object.
 """
 from __future__ import annotations
 
@@ -28,6 +31,9 @@ DRIVER = os.path.join(BINDIR, "mi_driver")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I" + INCLUDE, "-I" + CSRC]
+RDC_UNITS = {"mi_descr_persist.cu", "mi_pwalk_none.cu", "mi_pwalk_reference.cu", "mi_pwalk_reference_serial.cu",
+             "mi_pwalk_partial.cu"}
+DLINK = os.path.join(BUILD, "mi_rdc_dlink.o")
 
 
 def nvcc() -> str:
@@ -46,7 +52,8 @@ def _compile(src: str, verbose: bool) -> str:
     obj = os.path.join(BUILD, os.path.basename(src)[:-3] + ".o")
     if os.path.exists(obj) and os.path.getmtime(obj) >= max(os.path.getmtime(src), _deps()):
         return obj
-    cmd = [nvcc(), *ARCH, *NVCC_FLAGS, "-c", src, "-o", obj]
+    cmd = [nvcc(), *ARCH, *NVCC_FLAGS, *(["-rdc=true"] if os.path.basename(src) in RDC_UNITS else []), "-c", src,
+           "-o", obj]
     if verbose:
         cmd.insert(1, "-Xptxas=-v")
     out = subprocess.run(cmd, capture_output=True, text=True)
@@ -65,6 +72,13 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
     jobs = jobs or min(len(srcs), os.cpu_count() or 4)
     with ThreadPoolExecutor(max_workers=jobs) as ex:
         objs = list(ex.map(lambda s: _compile(s, verbose), srcs))
+    rdc = [o for s, o in zip(srcs, objs) if os.path.basename(s) in RDC_UNITS]
+    if rdc and (not os.path.exists(DLINK) or os.path.getmtime(DLINK) < max(os.path.getmtime(o) for o in rdc)):
+        out = subprocess.run([nvcc(), *ARCH, "-Xcompiler", "-fPIC", "-dlink", *rdc, "-o", DLINK], capture_output=True,
+                             text=True)
+        if out.returncode != 0:
+            raise RuntimeError("device link failed:\n" + out.stderr[-4000:])
+    objs = objs + ([DLINK] if rdc else [])
     if not os.path.exists(LIB) or os.path.getmtime(LIB) < max(os.path.getmtime(o) for o in objs):
         cmd = [nvcc(), *ARCH, "-shared", "-o", LIB, *objs]
         out = subprocess.run(cmd, capture_output=True, text=True)

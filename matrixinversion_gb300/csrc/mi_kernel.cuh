@@ -88,8 +88,10 @@ constexpr long long kWaitLimit = 4000000000LL;
 // tensor-core wait timed out (the MI_DEVERR_* flags of mi_inverse.h).  Every
 // translation unit that includes this header is a module of its own with its
 // own copy, so each registers a host reader of its copy when the library
-// loads; mi_device_error() reads them all.
-__device__ int g_device_error;
+// loads; mi_device_error() reads them all.  (Internal linkage: units
+// compiled as relocatable device code and linked together keep one copy
+// each as well.)
+static __device__ int g_device_error;
 
 using device_error_reader = cudaError_t (*)(int* flags, bool clear);
 bool register_device_error_reader(device_error_reader fn);   // mi_api.cu
@@ -116,8 +118,8 @@ cudaError_t read_device_error(int* flags, bool clear) {
 // completes, nothing is in flight, and the wait runs out after the limit.
 // Read once per launch by mi_inverse_kernel and mi_wide_kernel; set through
 // mi_set_wait_test.
-__device__ long long g_wait_limit = kWaitLimit;
-__device__ int g_wait_arm_only = 0;
+static __device__ long long g_wait_limit = kWaitLimit;
+static __device__ int g_wait_arm_only = 0;
 
 using wait_test_setter = cudaError_t (*)(long long limit, int arm_only);
 bool register_wait_test_setter(wait_test_setter fn);   // mi_api.cu
@@ -244,7 +246,7 @@ __host__ __device__ constexpr PrioTable make_prio_table() {
     return tab;
 }
 
-__constant__ PrioTable c_prio = make_prio_table();
+static __constant__ PrioTable c_prio = make_prio_table();
 
 // ---------------------------------------------------------------------------
 // Small helpers.
@@ -1168,10 +1170,12 @@ struct WarpSmem {
     float* outb;
     float* scr0;
     uint64_t* bar;
-    __device__ __forceinline__ WarpSmem(unsigned char* smem_raw, int warp) {
+    // warp `warp`'s region at a pitch of `pitch` floats (a multiple of 256)
+    // from the first 1 KB boundary of the dynamic shared memory
+    __device__ __forceinline__ WarpSmem(unsigned char* smem_raw, int warp, int pitch = KGeom<N, L, MODE>::kWarp) {
         using K = KGeom<N, L, MODE>;
         const uintptr_t base = (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023);
-        slot = reinterpret_cast<float*>(base) + (size_t)warp * K::kWarp;
+        slot = reinterpret_cast<float*>(base) + (size_t)warp * pitch;
         outb = slot + K::oOut;
         scr0 = slot + K::oScr;
         bar = reinterpret_cast<uint64_t*>(slot + K::oBar);
@@ -1313,40 +1317,33 @@ __global__ void __launch_bounds__(256, lane_min_blocks(N, L)) mi_inverse_kernel(
     if (lane == 0) bulk_wait_all();
 }
 
-// ---------------------------------------------------------------------------
-// Indexed batch (descriptor buckets): the matrices of one (n, mode) bucket are
-// list[range[0] .. range[0] + range[1]) -- descriptor indices -- at
-// base + offsets[index].  Each matrix moves in by a 1-D bulk copy when its
-// address allows (16-byte aligned, n*n a multiple of 4), else element by
-// element with asynchronous copies; results leave with plain stores.  Pivots
-// go to perm_out[index * 32 ..], info to info_out[index].
-// ---------------------------------------------------------------------------
+// One warp's walk over the groups g, g + gstride, ... (< g_end) of one
+// bucket, whose descriptor indices are list[start .. start + count).  The
+// warp's region `sm` holds the copy mbarrier only for the walk: it is
+// initialised here and invalidated before a normal return, so the region can
+// take another geometry afterwards.  Returns false when a copy wait ran out
+// (the device error word is set; the warp must take no more work).
 template <int N, int L, int MODE>
-__global__ void __launch_bounds__(256, lane_min_blocks(N, L)) mi_inverse_indexed_kernel(float* __restrict__ base,
-                                                                    const long long* __restrict__ offsets,
-                                                                    const int* __restrict__ list,
-                                                                    const long long* __restrict__ range,
-                                                                    int32_t* __restrict__ perm_out,
-                                                                    int32_t* __restrict__ info_out) {
+__device__ __forceinline__ bool indexed_walk(const WarpSmem<N, L, MODE>& sm, int lane, float* __restrict__ base,
+                                             const long long* __restrict__ offsets, const int* __restrict__ list,
+                                             long long start, long long count, long long g, long long g_end,
+                                             long long gstride, int32_t* __restrict__ perm_out,
+                                             int32_t* __restrict__ info_out) {
     using G = GeomN<N, L, MODE>;
     using K = KGeom<N, L, MODE>;
     constexpr int NN = N * N, R = G::R, C = G::C, M = G::M;
-    extern __shared__ unsigned char smem_raw[];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int W = blockDim.x >> 5;
-    const WarpSmem<N, L, MODE> sm(smem_raw, warp);
     const int mslot = lane / L;
-    const long long start = range[0], count = range[1];
-    if (count <= 0) return;
-
+    __syncwarp();
     if (lane == 0) {
         mbar_init(sm.bar, 1);
         fence_mbar_init();
+        // the region may hold data of an earlier walk, read and written
+        // through the generic proxy, where the first bulk copy lands
+        fence_proxy_async();
     }
     __syncwarp();
     const bool base16 = (reinterpret_cast<uintptr_t>(base) & 15u) == 0;
-    const long long groups = (count + M - 1) / M;
-    const long long gstride = (long long)gridDim.x * W;
+    const long long groups = g_end;
 
     // descriptor index of matrix m of group g (-1 past the end of the bucket)
     auto index_of = [&](long long g, int m) -> long long {
@@ -1382,7 +1379,6 @@ __global__ void __launch_bounds__(256, lane_min_blocks(N, L)) mi_inverse_indexed
         return bytes != 0;
     };
 
-    long long g = (long long)blockIdx.x * W + warp;
     uint32_t phase = 0;
     unsigned round = 0;
     bool timed_out = false;
@@ -1441,6 +1437,37 @@ __global__ void __launch_bounds__(256, lane_min_blocks(N, L)) mi_inverse_indexed
         mbar_wait(sm.bar, phase & 1u, kWaitLimit);
     }
     if (lane == 0) bulk_wait_all();
+    __syncwarp();
+    if (!timed_out && lane == 0) mbar_inval(sm.bar);
+    __syncwarp();
+    return !timed_out;
+}
+
+// ---------------------------------------------------------------------------
+// Indexed batch (descriptor buckets): the matrices of one (n, mode) bucket are
+// list[range[0] .. range[0] + range[1]) -- descriptor indices -- at
+// base + offsets[index].  Each matrix moves in by a 1-D bulk copy when its
+// address allows (16-byte aligned, n*n a multiple of 4), else element by
+// element with asynchronous copies; results leave with plain stores.  Pivots
+// go to perm_out[index * 32 ..], info to info_out[index].
+// ---------------------------------------------------------------------------
+template <int N, int L, int MODE>
+__global__ void __launch_bounds__(256, lane_min_blocks(N, L)) mi_inverse_indexed_kernel(float* __restrict__ base,
+                                                                    const long long* __restrict__ offsets,
+                                                                    const int* __restrict__ list,
+                                                                    const long long* __restrict__ range,
+                                                                    int32_t* __restrict__ perm_out,
+                                                                    int32_t* __restrict__ info_out) {
+    extern __shared__ unsigned char smem_raw[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int W = blockDim.x >> 5;
+    const long long start = range[0], count = range[1];
+    if (count <= 0) return;
+    const long long groups = (count + GeomN<N, L, MODE>::M - 1) / GeomN<N, L, MODE>::M;
+    const long long g = (long long)blockIdx.x * W + warp;
+    if (g >= groups) return;
+    indexed_walk<N, L, MODE>(WarpSmem<N, L, MODE>(smem_raw, warp), lane, base, offsets, list, start, count, g, groups,
+                             (long long)gridDim.x * W, perm_out, info_out);
 }
 
 // Dynamic shared memory for a block of `warps` warps (1 KB of slack for the

@@ -1,0 +1,7 @@
+// Walks of the single persistent descriptor launch for pivot mode none,
+// n = 1..32 (relocatable device code, linked with mi_descr_persist.cu).
+#include "mi_persist.cuh"
+
+namespace mi {
+MI_PWALK_EACH_N(MI_PWALK_DEF, 0)
+}  // namespace mi

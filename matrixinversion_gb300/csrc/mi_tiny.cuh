@@ -419,6 +419,26 @@ __global__ void __launch_bounds__(tiny_threads<N>()) mi_tiny_kernel(float* __res
     }
 }
 
+// One matrix of a descriptor bucket in registers (n = 1, 2): descriptor
+// index idx at base + offsets[idx].
+template <int N, int MODE>
+__device__ __forceinline__ void tiny_indexed_one(float* __restrict__ base, const long long* __restrict__ offsets,
+                                                 int idx, int32_t* __restrict__ perm_out,
+                                                 int32_t* __restrict__ info_out) {
+    float* src = base + offsets[idx];
+    float a[N][N], x[N][N];
+#pragma unroll
+    for (int e = 0; e < N * N; e++) a[e / N][e % N] = src[e];
+    int win[N], info;
+    tiny_invert<N, MODE>(a, x, win, info);
+    tiny_store<N>(src, x, win, false);
+    if (perm_out != nullptr) {
+#pragma unroll
+        for (int i = 0; i < N; i++) perm_out[(long long)idx * 32 + i] = win[i];
+    }
+    if (info_out != nullptr) info_out[idx] = info;
+}
+
 // Descriptor bucket: list[range[0] .. range[0] + range[1]) at base + offsets[i].
 template <int N, int MODE>
 __global__ void __launch_bounds__(256) mi_tiny_indexed_kernel(float* __restrict__ base,
@@ -429,42 +449,42 @@ __global__ void __launch_bounds__(256) mi_tiny_indexed_kernel(float* __restrict_
                                                               int32_t* __restrict__ info_out) {
     const long long start = range[0], count = range[1];
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < count;
-         t += (long long)gridDim.x * blockDim.x) {
-        const int idx = list[start + t];
-        float* src = base + offsets[idx];
-        float a[N][N], x[N][N];
-#pragma unroll
-        for (int e = 0; e < N * N; e++) a[e / N][e % N] = src[e];
-        int win[N], info;
-        tiny_invert<N, MODE>(a, x, win, info);
-        tiny_store<N>(src, x, win, false);
-        if (perm_out != nullptr) {
-#pragma unroll
-            for (int i = 0; i < N; i++) perm_out[(long long)idx * 32 + i] = win[i];
-        }
-        if (info_out != nullptr) info_out[idx] = info;
+         t += (long long)gridDim.x * blockDim.x)
+        tiny_indexed_one<N, MODE>(base, offsets, list[start + t], perm_out, info_out);
+}
+
+// One warp's walk over the groups g, g + gstride, ... (< g_end) of 32 list
+// entries of a bucket (lane = entry), n = 1, 2.
+template <int N, int MODE>
+__device__ __forceinline__ void tiny_indexed_walk(int lane, float* __restrict__ base,
+                                                  const long long* __restrict__ offsets, const int* __restrict__ list,
+                                                  long long start, long long count, long long g, long long g_end,
+                                                  long long gstride, int32_t* __restrict__ perm_out,
+                                                  int32_t* __restrict__ info_out) {
+    for (; g < g_end; g += gstride) {
+        const long long t = g * 32 + lane;
+        if (t < count) tiny_indexed_one<N, MODE>(base, offsets, list[start + t], perm_out, info_out);
     }
 }
 
-// Descriptor bucket, n > 8: each warp takes 32 list entries; the matrices
-// arrive one after another as coalesced 4-byte copies of their n * n floats
-// into the slots (pitch P), every copy in flight before the wait, and leave
-// the same way after each thread has inverted its slot.
+template <int N>
+__host__ __device__ constexpr int tiny_slot_floats() { return 32 * tiny_pitch<N>(); }
+
+// One warp's walk over the groups g, g + gstride, ... (< g_end) of 32 list
+// entries of a bucket through its stage `st` (tiny_slot_floats<N>() floats):
+// the matrices arrive one after another as coalesced 4-byte copies of their
+// n * n floats into the slots (pitch P), every copy in flight before the
+// wait, and leave the same way after each thread has inverted its slot.
 template <int N, int MODE>
-__global__ void __launch_bounds__(tiny_threads<N>()) mi_tiny_slot_indexed_kernel(float* __restrict__ base,
-                                                                                const long long* __restrict__ offsets,
-                                                                                const int* __restrict__ list,
-                                                                                const long long* __restrict__ range,
-                                                                                int32_t* __restrict__ perm_out,
-                                                                                int32_t* __restrict__ info_out) {
-    constexpr int NN = N * N, P = tiny_pitch<N>(), W = tiny_warps<N>();
+__device__ __forceinline__ void tiny_slot_walk(float* st, int lane, float* __restrict__ base,
+                                               const long long* __restrict__ offsets, const int* __restrict__ list,
+                                               long long start, long long count, long long g, long long g_end,
+                                               long long gstride, int32_t* __restrict__ perm_out,
+                                               int32_t* __restrict__ info_out) {
+    constexpr int NN = N * N, P = tiny_pitch<N>();
     constexpr int Q = (NN + 31) / 32;                   // copies per lane per matrix
-    __shared__ float stage[W][32 * P];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    float* st = stage[warp];
-    const long long start = range[0], count = range[1];
-    const long long wstride = (long long)gridDim.x * W * 32;
-    for (long long t0 = ((long long)blockIdx.x * W + warp) * 32; t0 < count; t0 += wstride) {
+    for (; g < g_end; g += gstride) {
+        const long long t0 = g * 32;
         const long long t = t0 + lane;
         const bool mine = t < count;
         const int idx = mine ? list[start + t] : 0;
@@ -501,6 +521,23 @@ __global__ void __launch_bounds__(tiny_threads<N>()) mi_tiny_slot_indexed_kernel
         }
         __syncwarp();
     }
+}
+
+// Descriptor bucket, n > 8: each warp takes 32 list entries at a time
+// (tiny_slot_walk).
+template <int N, int MODE>
+__global__ void __launch_bounds__(tiny_threads<N>()) mi_tiny_slot_indexed_kernel(float* __restrict__ base,
+                                                                                const long long* __restrict__ offsets,
+                                                                                const int* __restrict__ list,
+                                                                                const long long* __restrict__ range,
+                                                                                int32_t* __restrict__ perm_out,
+                                                                                int32_t* __restrict__ info_out) {
+    constexpr int W = tiny_warps<N>();
+    __shared__ float stage[W][tiny_slot_floats<N>()];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const long long start = range[0], count = range[1];
+    tiny_slot_walk<N, MODE>(stage[warp], lane, base, offsets, list, start, count, (long long)blockIdx.x * W + warp,
+                            (count + 31) / 32, (long long)gridDim.x * W, perm_out, info_out);
 }
 
 template <int N, int MODE>

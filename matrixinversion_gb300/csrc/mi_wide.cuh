@@ -367,28 +367,24 @@ __device__ __forceinline__ void cp_async_16_cg(float* dst, const float* src) {
 // bytes when its address allows, else 4) and its rows leave from one output
 // buffer by plain stores (16 bytes when aligned).  Pivots go to
 // perm_out[idx * 32 ..], info to info_out[idx].
+//
+// wide_gather_walk is one warp's walk over the groups g, g + gstride, ...
+// (< g_end) of four matrices, in the warp's region `slot` (WideGeom::kWarp
+// floats, 1 KB aligned); mi_wide_gather_kernel runs it on persistent warps.
 template <int MODE, bool IDX>
-__global__ void __launch_bounds__(WideGeom::kThreadsMax, 1)
-    mi_wide_gather_kernel(float* __restrict__ base, const long long* __restrict__ offsets,
-                          const int* __restrict__ list, const long long* __restrict__ range, long long batch,
-                          int32_t* __restrict__ perm_out, int32_t* __restrict__ info_out) {
+__device__ __forceinline__ void wide_gather_walk(float* slot, int lane, float* __restrict__ base,
+                                                 const long long* __restrict__ offsets, const int* __restrict__ list,
+                                                 long long start, long long count, long long g, long long g_end,
+                                                 long long gstride, int32_t* __restrict__ perm_out,
+                                                 int32_t* __restrict__ info_out) {
     using G = WideGeom;
     static_assert(MODE != kModePartial, "partial pivoting has its own kernels");
-    extern __shared__ unsigned char smem_raw[];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int W = blockDim.x >> 5;
-    const uintptr_t sbase = (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023);
-    float* slot = reinterpret_cast<float*>(sbase) + (size_t)warp * G::kWarp;
     float* outb = slot + G::oOut;
     float* scr0 = slot + G::oScr;
     const int ms = lane >> 3, s = lane & 7;
     const int rg = s & 1, cg = s >> 1;
     const int* win = reinterpret_cast<const int*>(scr0 + ms * G::kScr + G::oWin);
-    const long long start = IDX ? range[0] : 0;
-    const long long count = IDX ? range[1] : batch;
-    if (count <= 0) return;
-    const long long groups = (count + G::M - 1) / G::M;
-    const long long gstride = (long long)gridDim.x * W;
+    const long long groups = g_end;
 
     // descriptor index of matrix m of group g (-1 past the end) and its address
     auto index_of = [&](long long g, int m) -> long long {
@@ -417,7 +413,6 @@ __global__ void __launch_bounds__(WideGeom::kThreadsMax, 1)
         cp_async_commit();
     };
 
-    long long g = (long long)blockIdx.x * W + warp;
     if (g < groups) issue(g);
     while (g < groups) {
         cp_async_wait_all();
@@ -459,6 +454,24 @@ __global__ void __launch_bounds__(WideGeom::kThreadsMax, 1)
         wide_perm_info(scr0 + ms * G::kScr, s, lane & ~7, index_of(g, ms), perm_out, info_out, win);
         g = gn;
     }
+}
+
+template <int MODE, bool IDX>
+__global__ void __launch_bounds__(WideGeom::kThreadsMax, 1)
+    mi_wide_gather_kernel(float* __restrict__ base, const long long* __restrict__ offsets,
+                          const int* __restrict__ list, const long long* __restrict__ range, long long batch,
+                          int32_t* __restrict__ perm_out, int32_t* __restrict__ info_out) {
+    using G = WideGeom;
+    extern __shared__ unsigned char smem_raw[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int W = blockDim.x >> 5;
+    const uintptr_t sbase = (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023);
+    float* slot = reinterpret_cast<float*>(sbase) + (size_t)warp * G::kWarp;
+    const long long start = IDX ? range[0] : 0;
+    const long long count = IDX ? range[1] : batch;
+    if (count <= 0) return;
+    wide_gather_walk<MODE, IDX>(slot, lane, base, offsets, list, start, count, (long long)blockIdx.x * W + warp,
+                                (count + G::M - 1) / G::M, (long long)gridDim.x * W, perm_out, info_out);
 }
 
 }  // namespace mi

@@ -3,8 +3,11 @@
 Matrix i of a packed float32 buffer starts at offsets[i] (floats) and is
 n_i x n_i, row-major; flags[i] is its pivot mode (0 none, 1 reference,
 2 reference_serial, 3 partial).  One call buckets the table by (n, flag) on
-the GPU and runs one persistent launch per bucket -- all stream-ordered, so
-the call can be captured into a CUDA graph (DescrGraph).
+the GPU and runs one persistent launch per bucket present (the default) or,
+after set_chunk(c > 0), ONE persistent launch whose warps take chunks of
+groups of every bucket from a device counter, largest n first -- all
+stream-ordered, so the call can be captured into a CUDA graph (DescrGraph).
+Either way every matrix gets the bits of the contiguous call.
 """
 from __future__ import annotations
 
@@ -38,6 +41,17 @@ def pack(matrices, align: int = 4):
 
 def unpack(packed, offsets, ns):
     return [np.asarray(packed[o: o + n * n]).reshape(n, n) for o, n in zip(offsets, ns)]
+
+
+def set_chunk(chunk_floats: int) -> None:
+    """Form of the descriptor call: 0 (the default) = one launch per (n, mode)
+    bucket; c > 0 = the single persistent launch with chunks of about c input
+    floats (1 to 8 groups).  Process-wide."""
+    _lib.check(_lib.load().mi_set_descr_chunk(int(chunk_floats)))
+
+
+def get_chunk() -> int:
+    return int(_lib.load().mi_get_descr_chunk())
 
 
 def workspace_bytes(count: int) -> int:
@@ -160,10 +174,12 @@ def uneven_batch(count: int, align: int = 4, seed: int = 0, pivot_flag: int = 1,
     return packed, offsets, ns, flags
 
 
-def bench_uneven(count: int = 1_000_000, align: int = 4, iters: int = 10, seed: int = 0, pivot_flag: int = 1):
-    """Descriptor call (eager and graph-captured) vs one contiguous launch per
-    (n, flag) bucket over the same matrices pre-sorted; kernel time by CUDA
-    events, each run on a fresh copy of the inputs."""
+def bench_uneven(count: int = 1_000_000, align: int = 4, iters: int = 10, seed: int = 0, pivot_flag: int = 1,
+                 chunks=(16384,)):
+    """Descriptor call (eager and graph-captured; the single persistent launch
+    at each chunk size of `chunks`, and one launch per bucket) vs one
+    contiguous launch per (n, flag) bucket over the same matrices pre-sorted;
+    kernel time by CUDA events, each run on a fresh copy of the inputs."""
     import torch
 
     import matrixinversion_gb300 as mi
@@ -193,9 +209,17 @@ def bench_uneven(count: int = 1_000_000, align: int = 4, iters: int = 10, seed: 
     reset = lambda: packed.copy_(src)
     eager = lambda: batched_inverse_descr_(packed, offsets, ns, flags, info=info, workspace=ws, n_mask=n_mask,
                                            mode_mask=mode_mask)
-    t_eager = timed(eager, reset)
-    graph = DescrGraph(packed, offsets, ns, flags, info=info, n_mask=n_mask, mode_mask=mode_mask)
-    t_graph = timed(graph.replay, reset)
+    saved = get_chunk()
+    forms = {}
+    try:
+        for c in [*chunks, 0]:
+            set_chunk(c)
+            t_e = timed(eager, reset)
+            graph = DescrGraph(packed, offsets, ns, flags, info=info, n_mask=n_mask, mode_mask=mode_mask)
+            forms[c] = (t_e, timed(graph.replay, reset))
+    finally:
+        set_chunk(saved)
+    t_eager, t_graph = forms[chunks[0]]
     # per-bucket baseline: the same matrices sorted into contiguous buckets
     host = src.cpu().numpy()
     nh, fh, oh = ns.cpu().numpy(), flags.cpu().numpy(), offsets.cpu().numpy()
@@ -219,7 +243,10 @@ def bench_uneven(count: int = 1_000_000, align: int = 4, iters: int = 10, seed: 
 
     t_bucket = timed(per_bucket, breset)
     bytes_alg = float((8 * ns.double() ** 2 + 4 * ns.double() + 4).sum() + 16 * count)
-    return {"count": count, "align": align, "eager_ms": t_eager, "graph_ms": t_graph, "per_bucket_ms": t_bucket,
+    return {"count": count, "align": align, "chunk_floats": chunks[0], "eager_ms": t_eager, "graph_ms": t_graph,
+            "launch_per_bucket": {"eager_ms": forms[0][0], "graph_ms": forms[0][1]},
+            "chunk_sweep": {str(c): {"eager_ms": e, "graph_ms": g} for c, (e, g) in forms.items() if c},
+            "per_bucket_ms": t_bucket,
             "buckets": len(buckets), "matrices_per_s_graph": count / t_graph * 1e3,
             "bytes_per_launch": bytes_alg, "GBs_graph": bytes_alg / t_graph / 1e6,
             "singular": int((info != 0).sum().item())}
@@ -234,16 +261,18 @@ def main(argv=None):
     p.add_argument("--align", default="4,1")
     p.add_argument("--tune", action="store_true", help="autotune threads per block first")
     p.add_argument("--iters", type=int, default=10)
+    p.add_argument("--chunks", default="16384", help="persistent-launch chunk sizes (floats), the first reported")
     a = p.parse_args(argv)
     if a.tune:
         from . import autotune
 
         autotune.tune(range(2, 33), ("none", "reference"), batch=131072, iters=3)
     for al in a.align.split(","):
-        print(json.dumps({"tuned": a.tune, **bench_uneven(a.count, int(al), a.iters)}), flush=True)
+        chunks = tuple(int(c) for c in a.chunks.split(","))
+        print(json.dumps({"tuned": a.tune, **bench_uneven(a.count, int(al), a.iters, chunks=chunks)}), flush=True)
 
 
-__all__ = ["pack", "unpack", "workspace_bytes", "masks", "batched_inverse_descr_", "DescrGraph", "pivot_mode",
+__all__ = ["pack", "unpack", "set_chunk", "get_chunk", "workspace_bytes", "masks", "batched_inverse_descr_", "DescrGraph", "pivot_mode",
            "uneven_batch", "bench_uneven"]
 
 if __name__ == "__main__":

@@ -185,6 +185,13 @@ def test_noalloc_and_descriptor_argument_checks_without_gpu(lib):
     assert d(p, big, p, p, p, None, None, 4, 0, 0, p, need - 1, None) == _lib.MI_ERR_INVALID_VALUE
     for count in (0, 1, 1000, 262144):
         assert lib.mi_descr_workspace_bytes(count) == (4096 + 4 * count + 255) // 256 * 256
+    # the descriptor form: 0 (default) one launch per bucket, c > 0 the
+    # single persistent launch with chunks of about c floats
+    saved = lib.mi_get_descr_chunk()
+    assert saved == 0
+    assert lib.mi_set_descr_chunk(-1) == _lib.MI_ERR_INVALID_VALUE and lib.mi_get_descr_chunk() == saved
+    assert lib.mi_set_descr_chunk(16384) == _lib.MI_OK and lib.mi_get_descr_chunk() == 16384
+    assert lib.mi_set_descr_chunk(saved) == _lib.MI_OK and lib.mi_get_descr_chunk() == saved
     na = lib.mi_inverse_descr_noalloc_f32
     assert na(None, 0, None, None, None, None, None, 0, 0, 0, None) == _lib.MI_OK
     assert na(None, 0, None, None, None, None, None, -5, 0, 0, None) == _lib.MI_ERR_INVALID_VALUE

@@ -3,7 +3,9 @@
 Every matrix must come back bit-for-bit equal to the contiguous kernel's
 result for the same matrix (same arithmetic, different data movement), with
 the same pivots; malformed descriptors are reported and left untouched; the
-call replays correctly from a CUDA graph.
+call replays correctly from a CUDA graph.  Each check runs in both forms of
+the call: the single persistent launch (chunks of the default size) and one
+launch per (n, mode) bucket.
 """
 import numpy as np
 import pytest
@@ -11,6 +13,16 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 MODES = ["none", "reference", "reference_serial", "partial"]
+
+
+@pytest.fixture(params=["persistent", "per_bucket"])
+def form(request):
+    from matrixinversion_gb300 import descr
+
+    saved = descr.get_chunk()
+    descr.set_chunk(16384 if request.param == "persistent" else 0)
+    yield request.param
+    descr.set_chunk(saved)
 
 
 def make_case(oracle, count, seed, nmin=1, nmax=32):
@@ -39,7 +51,7 @@ def contiguous_results(mi, mats, flags):
 
 
 @pytest.mark.parametrize("align", [4, 1])
-def test_descriptor_batch_matches_contiguous(mi_gpu, oracle, align):
+def test_descriptor_batch_matches_contiguous(mi_gpu, oracle, align, form):
     import torch
 
     from matrixinversion_gb300 import descr
@@ -65,7 +77,7 @@ def test_descriptor_batch_matches_contiguous(mi_gpu, oracle, align):
             assert np.array_equal(perm[i, : A.shape[0]], oracle.pivots(A[None], MODES[f])[0])
 
 
-def test_malformed_descriptors_and_masks(mi_gpu, oracle):
+def test_malformed_descriptors_and_masks(mi_gpu, oracle, form):
     import torch
 
     from matrixinversion_gb300 import descr
@@ -104,7 +116,7 @@ def test_malformed_descriptors_and_masks(mi_gpu, oracle):
     assert np.array_equal(got[0], mats[0])
 
 
-def test_descriptor_graph_replay(mi_gpu, oracle):
+def test_descriptor_graph_replay(mi_gpu, oracle, form):
     import torch
 
     from matrixinversion_gb300 import descr
@@ -123,3 +135,71 @@ def test_descriptor_graph_replay(mi_gpu, oracle):
         got = descr.unpack(d_packed.cpu().numpy(), offsets, ns_)
         for i in range(len(mats)):
             assert np.array_equal(got[i], want[i]), i
+
+
+@pytest.mark.parametrize("chunk", [1, 5000, 1 << 22])
+def test_persistent_chunk_sizes(mi_gpu, oracle, chunk):
+    """One group per chunk (the smallest chunk), mid-size chunks that split
+    buckets between warps, and the largest (eight groups): the bits of the
+    contiguous call every time, densely packed (4-byte aligned matrices)."""
+    import torch
+
+    from matrixinversion_gb300 import descr
+
+    mats, ns, flags = make_case(oracle, 500, 31)
+    packed, offsets, ns_ = descr.pack(mats, align=1)
+    want, wperm, winfo = contiguous_results(mi_gpu, mats, flags)
+    saved = descr.get_chunk()
+    try:
+        descr.set_chunk(chunk)
+        d_packed = torch.from_numpy(packed).cuda()
+        perm = torch.full((len(mats), 32), -7, dtype=torch.int32, device="cuda")
+        info = torch.full((len(mats),), -7, dtype=torch.int32, device="cuda")
+        descr.batched_inverse_descr_(d_packed, torch.from_numpy(offsets).cuda(), torch.from_numpy(ns_).cuda(),
+                                     torch.from_numpy(flags).cuda(), perm=perm, info=info)
+        torch.cuda.synchronize()
+    finally:
+        descr.set_chunk(saved)
+    got = descr.unpack(d_packed.cpu().numpy(), offsets, ns_)
+    perm, info = perm.cpu().numpy(), info.cpu().numpy()
+    for i, n in enumerate(ns_):
+        assert np.array_equal(got[i], want[i]), (i, n, flags[i])
+        assert np.array_equal(perm[i, :n], wperm[i]), i
+        assert info[i] == winfo[i]
+
+
+def test_persistent_equals_per_bucket_large(mi_gpu):
+    """60,000 matrices, every n = 1..32 and every pivot mode, some singular:
+    the single persistent launch (many chunks per bucket, thousands of warps)
+    and one launch per bucket give the same bits, pivots and info."""
+    import torch
+
+    from matrixinversion_gb300 import descr
+
+    rng = np.random.RandomState(5)
+    count = 60000
+    ns = rng.randint(1, 33, size=count).astype(np.int32)
+    flags = rng.randint(0, 4, size=count).astype(np.int32)
+    offsets = np.zeros(count, dtype=np.int64)
+    offsets[1:] = np.cumsum(ns.astype(np.int64) ** 2)[:-1]
+    total = int(offsets[-1] + int(ns[-1]) ** 2)
+    src = torch.from_numpy(rng.uniform(-1, 1, size=total).astype(np.float32)).cuda()
+    for i in rng.choice(count, 50, replace=False):      # singular: a zero matrix
+        src[int(offsets[i]): int(offsets[i]) + int(ns[i]) ** 2] = 0.0
+    d_off, d_n, d_f = (torch.from_numpy(x).cuda() for x in (offsets, ns, flags))
+    saved = descr.get_chunk()
+    out = {}
+    try:
+        for c in (16384, 0):
+            descr.set_chunk(c)
+            d = src.clone()
+            perm = torch.full((count, 32), -7, dtype=torch.int32, device="cuda")
+            info = torch.full((count,), -7, dtype=torch.int32, device="cuda")
+            descr.batched_inverse_descr_(d, d_off, d_n, d_f, perm=perm, info=info)
+            torch.cuda.synchronize()
+            out[c] = (d, perm, info)
+    finally:
+        descr.set_chunk(saved)
+    assert torch.equal(out[16384][0].view(torch.int32), out[0][0].view(torch.int32))
+    assert torch.equal(out[16384][1], out[0][1]) and torch.equal(out[16384][2], out[0][2])
+    assert int((out[0][2] == -7).sum()) == 0 and int((out[0][2] != 0).sum()) >= 50
