@@ -252,6 +252,49 @@ def bench_uneven(count: int = 1_000_000, align: int = 4, iters: int = 10, seed: 
             "singular": int((info != 0).sum().item())}
 
 
+def bench_single_size(ns=(2, 8, 14, 16, 24, 31, 32), count: int = 131072, flag: int = 1, iters: int = 8,
+                      chunks=(1, 16384)):
+    """Descriptor calls over one size at a time (masks naming that size and
+    mode only): one launch per bucket against the single persistent launch
+    at each chunk size; kernel time by CUDA events (median after two
+    warm-ups), each run on a fresh copy of the inputs."""
+    import torch
+
+    saved = get_chunk()
+    rows = []
+    try:
+        for n in ns:
+            g = torch.Generator(device="cuda").manual_seed(n)
+            src = (torch.rand(count, n, n, generator=g, device="cuda") * 2 - 1).reshape(-1)
+            if flag == 0:
+                src.view(count, n, n).add_(n * torch.eye(n, device="cuda"))
+            d = src.clone()
+            offsets = torch.arange(count, dtype=torch.int64, device="cuda") * (n * n)
+            nsd = torch.full((count,), n, dtype=torch.int32, device="cuda")
+            fl = torch.full((count,), flag, dtype=torch.int32, device="cuda")
+            ws = torch.empty(workspace_bytes(count), dtype=torch.uint8, device="cuda")
+            info = torch.empty(count, dtype=torch.int32, device="cuda")
+            row = {"n": n, "flag": flag, "count": count}
+            for c in (0, *chunks):
+                set_chunk(c)
+                ts = []
+                for it in range(iters + 2):
+                    d.copy_(src)
+                    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                    e0.record()
+                    batched_inverse_descr_(d, offsets, nsd, fl, info=info, workspace=ws, n_mask=1 << (n - 1),
+                                           mode_mask=1 << flag)
+                    e1.record()
+                    torch.cuda.synchronize()
+                    if it >= 2:
+                        ts.append(e0.elapsed_time(e1))
+                row["per_bucket_ms" if c == 0 else f"persistent_{c}_ms"] = float(np.median(ts))
+            rows.append(row)
+    finally:
+        set_chunk(saved)
+    return rows
+
+
 def main(argv=None):
     import argparse
     import json
@@ -262,7 +305,15 @@ def main(argv=None):
     p.add_argument("--tune", action="store_true", help="autotune threads per block first")
     p.add_argument("--iters", type=int, default=10)
     p.add_argument("--chunks", default="16384", help="persistent-launch chunk sizes (floats), the first reported")
+    p.add_argument("--single-size", default="", help="sizes to time one at a time (both forms) instead")
     a = p.parse_args(argv)
+    if a.single_size:
+        chunks = tuple(int(c) for c in a.chunks.split(","))
+        for flag in (1, 0):
+            for row in bench_single_size(tuple(int(x) for x in a.single_size.split(",")), a.count, flag,
+                                         chunks=chunks):
+                print(json.dumps(row), flush=True)
+        return
     if a.tune:
         from . import autotune
 
@@ -273,7 +324,7 @@ def main(argv=None):
 
 
 __all__ = ["pack", "unpack", "set_chunk", "get_chunk", "workspace_bytes", "masks", "batched_inverse_descr_", "DescrGraph", "pivot_mode",
-           "uneven_batch", "bench_uneven"]
+           "uneven_batch", "bench_uneven", "bench_single_size"]
 
 if __name__ == "__main__":
     import sys
