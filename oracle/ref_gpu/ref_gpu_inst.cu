@@ -1,9 +1,10 @@
 // Test infrastructure (never the product): explicit instantiations of the
-// reference's own GPU kernel, batched_lu_subwarp
-// (parallel_pivot/luBatchedInplace.cuh:127-198), compiled unchanged from the
-// reference tree into a device-only cubin (oracle/Makefile, target ref_gpu)
-// so that it can be timed on the GPU beside this project's kernels
-// (oracle/ref_gpu.py).  The template arguments follow the reference's driver
+// reference's own GPU kernel, batched_lu_subwarp -- parallel_pivot
+// (luBatchedInplace.cuh:127-198), serial_pivot (:104-170) and templated
+// (:78-121), one cubin each, all with this file and the variant's directory
+// on the include path -- compiled unchanged from the reference tree into
+// device-only cubins (oracle/Makefile, target ref) so that they can be timed
+// on the GPU beside this project's kernels (oracle/ref_gpu.py).  The template arguments follow the reference's driver
 // (parallel_pivot/luBatchedInplace.cu:4-11: threads per matrix = n, matrices
 // per block = NUMTHREADS / n) with NUMTHREADS from parallel_pivot/run.py:187-222
 // (32 for n = 4, 8, 16; n for n > 16).  numMatrices is a template argument:
@@ -22,3 +23,4 @@ MI_REF_INST(32, 1, 1000000)
 MI_REF_INST(8, 4, 4096)
 MI_REF_INST(16, 2, 4096)
 MI_REF_INST(32, 1, 4096)
+MI_REF_INST(32, 1, 1000)

@@ -1,39 +1,53 @@
-"""This project's kernel against the reference's own GPU kernel
-(batched_lu_subwarp, parallel_pivot/luBatchedInplace.cuh:127-198, compiled
+"""This project's kernels against the reference's own GPU kernels
+(batched_lu_subwarp of parallel_pivot, serial_pivot and templated, compiled
 unchanged into oracle/_ref by `make -C oracle REF_ROOT=... ref`) on the same
-GPU and the same matrices.  The reference kernel keeps its pivots in shared
-memory, so the comparison is on the inverses: both must be the same A^-1 to
-within rounding, with residuals of the same size.  Skipped where the cubin was
-not built (it needs the reference sources at build time)."""
+GPU and the same matrices, in the matching pivot mode.  The reference kernels
+keep their pivots in shared memory, so the comparison is on the inverses:
+both must be the same A^-1 to within rounding, with residuals of the same
+size.  Skipped where the cubins were not built (they need the reference
+sources at build time)."""
 import numpy as np
 import pytest
 
 pytestmark = pytest.mark.gpu
 
 
+@pytest.mark.parametrize("mode", ["reference", "reference_serial", "none"])
 @pytest.mark.parametrize("n", [8, 16, 32])
-def test_matches_reference_gpu_kernel(mi_gpu, n):
+def test_matches_reference_gpu_kernel(mi_gpu, n, mode):
     import torch
 
     from oracle import ref_gpu
 
-    if not ref_gpu.available():
+    if not ref_gpu.available(mode):
         pytest.skip("reference GPU kernel not built (oracle/_ref)")
     count = 4096
     g = torch.Generator(device="cuda").manual_seed(700 + n)
     src = torch.rand(count, n, n, generator=g, device="cuda") * 2 - 1
+    if mode == "none":
+        src += n * torch.eye(n, device="cuda")
     X_ref = src.clone()
-    ref_gpu.RefKernels().invert_(X_ref)
+    ref_gpu.RefKernels(mode).invert_(X_ref)
     X_mi = src.clone()
-    mi_gpu.batched_inverse_(X_mi, "reference")
+    mi_gpu.batched_inverse_(X_mi, mode)
     torch.cuda.synchronize()
     r_ref = ref_gpu.residuals(src, X_ref, count).cpu().numpy()
     r_mi = ref_gpu.residuals(src, X_mi, count).cpu().numpy()
-    # same algorithm and pivot rule, different evaluation order: residuals of
-    # the same size (1,000,000 matrices per n measured 0.74-1.11x the
-    # reference kernel's median) and the same inverse to rounding
-    assert np.median(r_mi) <= 1.5 * np.median(r_ref)
-    assert np.median(r_ref) <= 1.5 * np.median(r_mi)
     rel = ((X_ref - X_mi).abs().amax((1, 2)) / X_ref.abs().amax((1, 2))).cpu().numpy()
-    assert np.median(rel) < 1e-4
     assert np.all(np.isfinite(X_mi.cpu().numpy()))
+    if mode == "none":
+        # diagonally dominant inputs: both inverses within a few units of
+        # FP32 of each other; the product-form Gauss-Jordan residual AX - I
+        # runs 1.2-3.0x the LU-and-triangular-inverses one (1,000,000
+        # matrices per n: medians 1.1e-7..5.2e-7 against 0.9e-7..1.7e-7),
+        # far inside the 1e-5 per-matrix bound of the no-pivot configuration
+        assert np.median(r_mi) <= 4.0 * np.median(r_ref)
+        assert np.all(r_mi < 1e-5) and np.all(r_ref < 1e-5)
+        assert np.max(rel) < 1e-5
+    else:
+        # the same pivot rule, different evaluation order: residuals of the
+        # same size (1,000,000 matrices per n measured 0.74-1.11x the
+        # reference kernel's median) and the same inverse to rounding
+        assert np.median(r_mi) <= 1.5 * np.median(r_ref)
+        assert np.median(r_ref) <= 1.5 * np.median(r_mi)
+        assert np.median(rel) < 1e-4
