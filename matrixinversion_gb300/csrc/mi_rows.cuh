@@ -144,7 +144,13 @@ __global__ void __launch_bounds__(32 * kRowsWarps, LN == 16 ? 3 : 2) mi_rows_par
 #pragma unroll
             for (int j = N; j < NC; j++) a[ri][j] = 0.0f;
         }
-        // ---- n steps of partial pivoting
+        // ---- n steps of partial pivoting.  The search of step k + 1 runs
+        // inside step k: as soon as the pivot row of step k is in the buffer,
+        // column k + 1 takes its update (the same fma the full update would
+        // give it), the keys of that column go into the two 16-lane maxima,
+        // and only then does the rest of step k's update run -- so the
+        // shuffle latency of the search overlaps the update's FMAs instead of
+        // heading the next step.
         int lp[R];
         bool placed[R];
 #pragma unroll
@@ -152,14 +158,15 @@ __global__ void __launch_bounds__(32 * kRowsWarps, LN == 16 ? 3 : 2) mi_rows_par
             lp[ri] = s + kRowsLanes * ri;
             placed[ri] = (s + kRowsLanes * ri >= N);
         }
-#pragma unroll
-        for (int k = 0; k < N; k++) {
-            // my candidate: the largest key, then the lowest logical row
+        // getrf's pivot of column kk over the rows not yet placed: the
+        // largest key, then the lowest logical row; returns (255 - logical
+        // row) << 8 | slot of the winner
+        auto search = [&](int kk) -> unsigned {
             unsigned bk = 0u;
             int bl = 255, bs = 0;
 #pragma unroll
             for (int ri = 0; ri < R; ri++) {
-                const unsigned key = placed[ri] ? 0u : rows_key(a[ri][k]);
+                const unsigned key = placed[ri] ? 0u : rows_key(a[ri][kk]);
                 if (key > bk || (key == bk && key != 0u && lp[ri] < bl)) {
                     bk = key;
                     bl = lp[ri];
@@ -168,7 +175,11 @@ __global__ void __launch_bounds__(32 * kRowsWarps, LN == 16 ? 3 : 2) mi_rows_par
             }
             const unsigned mx = rows_group_max<kRowsLanes>(bk);
             const unsigned cand = (bk != 0u && bk == mx) ? (((unsigned)(255 - bl) << 8) | (unsigned)bs) : 0u;
-            const unsigned best = rows_group_max<kRowsLanes>(cand);
+            return rows_group_max<kRowsLanes>(cand);
+        };
+        unsigned best = search(0);
+#pragma unroll
+        for (int k = 0; k < N; k++) {
             const int r = (int)(best & 0xffu);               // pivot slot
             const int lw = 255 - (int)(best >> 8);           // its logical row
 #pragma unroll
@@ -206,7 +217,16 @@ __global__ void __launch_bounds__(32 * kRowsWarps, LN == 16 ? 3 : 2) mi_rows_par
                 const float m = c * p;
                 nm[ri] = make_float2(-m, -m);
             }
-            // the pivot row streams through in 16-byte chunks (4 values live)
+            // column k + 1 first, then the search of step k + 1
+            const int k1 = k + 1;
+            if (k1 < N) {
+                const float w1 = rb[k1];
+#pragma unroll
+                for (int ri = 0; ri < R; ri++) a[ri][k1] = fmaf(nm[ri].x, w1, a[ri][k1]);
+                best = search(k1);
+            }
+            // the rest of the update: the pivot row streams through in 16-byte
+            // chunks (4 values live); column k + 1 is done
 #pragma unroll
             for (int q = 0; q < NC / 4; q++) {
                 float4 v = *reinterpret_cast<const float4*>(rb + 4 * q);
@@ -214,16 +234,30 @@ __global__ void __launch_bounds__(32 * kRowsWarps, LN == 16 ? 3 : 2) mi_rows_par
                 if (k == 4 * q + 1) v.y = 1.0f;
                 if (k == 4 * q + 2) v.z = 1.0f;
                 if (k == 4 * q + 3) v.w = 1.0f;
+                const bool d0 = k1 < N && k1 == 4 * q, d1 = k1 < N && k1 == 4 * q + 1;
+                const bool d2 = k1 < N && k1 == 4 * q + 2, d3 = k1 < N && k1 == 4 * q + 3;
 #pragma unroll
                 for (int ri = 0; ri < R; ri++) {
-                    float2 x0 = make_float2(a[ri][4 * q], a[ri][4 * q + 1]);
-                    float2 x1 = make_float2(a[ri][4 * q + 2], a[ri][4 * q + 3]);
-                    x0 = __ffma2_rn(nm[ri], make_float2(v.x, v.y), x0);
-                    x1 = __ffma2_rn(nm[ri], make_float2(v.z, v.w), x1);
-                    a[ri][4 * q] = x0.x;
-                    a[ri][4 * q + 1] = x0.y;
-                    a[ri][4 * q + 2] = x1.x;
-                    a[ri][4 * q + 3] = x1.y;
+                    if (!d0 && !d1) {
+                        float2 x0 = make_float2(a[ri][4 * q], a[ri][4 * q + 1]);
+                        x0 = __ffma2_rn(nm[ri], make_float2(v.x, v.y), x0);
+                        a[ri][4 * q] = x0.x;
+                        a[ri][4 * q + 1] = x0.y;
+                    } else if (d0) {
+                        a[ri][4 * q + 1] = fmaf(nm[ri].y, v.y, a[ri][4 * q + 1]);
+                    } else {
+                        a[ri][4 * q] = fmaf(nm[ri].x, v.x, a[ri][4 * q]);
+                    }
+                    if (!d2 && !d3) {
+                        float2 x1 = make_float2(a[ri][4 * q + 2], a[ri][4 * q + 3]);
+                        x1 = __ffma2_rn(nm[ri], make_float2(v.z, v.w), x1);
+                        a[ri][4 * q + 2] = x1.x;
+                        a[ri][4 * q + 3] = x1.y;
+                    } else if (d2) {
+                        a[ri][4 * q + 3] = fmaf(nm[ri].y, v.w, a[ri][4 * q + 3]);
+                    } else {
+                        a[ri][4 * q + 2] = fmaf(nm[ri].x, v.z, a[ri][4 * q + 2]);
+                    }
                 }
             }
         }
@@ -331,9 +365,10 @@ cudaError_t launch_rows_partial(float* a, int32_t* perm, int32_t* info, long lon
 // Measured on GB300 at 1,000,000 matrices against the lane-block kernel
 // (gj_step_partial, one matrix per warp above n = 16), same bits: n = 16
 // 1.63 -> 1.20 ms, 17 3.68 -> 2.59, 20 4.20 -> 2.65, 24 4.99 -> 4.21, 28
-// 6.33 -> 5.27, 32 6.99 -> 6.76; at n = 29..31 this kernel spills registers
-// and n = 31 was 5% slower.
+// 6.33 -> 5.27, 32 6.99 -> 6.76.  At n = 29..31 it spilled registers until
+// the search of each step moved into the previous one (154-158 registers
+// since, no spills).
 template <int N>
-__host__ __device__ constexpr bool rows_partial_enabled() { return N <= 28 || N == 32; }
+__host__ __device__ constexpr bool rows_partial_enabled() { return N >= kRowsMin; }
 
 }  // namespace mi
