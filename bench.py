@@ -277,12 +277,14 @@ def main():
         hI = torch.empty((batch,), dtype=torch.int32).pin_memory()
         from matrixinversion_gb300.host import link_bandwidth
 
-        for _ in range(2):
-            pipe.run(hA, args.pivot, hX, hP, hI)
-        # the link's rates just before and just after the timed steps: the
-        # host memory behind the link is shared with whatever else runs on the
-        # machine, and a rate that drops during the run shows up here
+        # the link's rates before the warm-up steps and just after the timed
+        # ones: the host memory behind the link is shared with whatever else
+        # runs on the machine, and a rate that drops during the run shows up
+        # here.  (The probe pins 2 GB of fresh host memory; the pipeline's
+        # warm-up steps run after it, not the timed ones.)
         link_before = link_bandwidth(dev)
+        for _ in range(3):
+            pipe.run(hA, args.pivot, hX, hP, hI)
         e2e_steps = max(1, min(args.steps, 5))
         step_times = []
         barrier()
