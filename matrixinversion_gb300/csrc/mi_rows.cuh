@@ -32,12 +32,13 @@ constexpr int kRowsMin = 16;        // smallest n of this kernel (partial pivoti
 
 // Lanes per matrix at size n: 16 (two matrices per warp, two rows per lane)
 // or 8 (four matrices per warp, up to four rows per lane).  Measured on GB300
-// at 1,000,000 matrices, same bits: 8 lanes take n = 18 from 2.92 to 2.12 ms
-// but are slower at n = 17 (3.10 against 2.59 ms), 20, 22, 24 (4.62 against
-// 4.21) and far slower from n = 25 up, where four whole rows per lane spill
-// (n = 32: 12.04 against 6.74 ms).
+// at 1,000,000 matrices, same bits, with each step's search inside the
+// previous step: 8 lanes at n = 17 1.69 against 2.09 ms, 18 1.82 against
+// 2.30, 19 2.02 against 2.70, 20 1.95 against 2.35.  (Before that change 8
+// lanes won only at n = 18; from n = 25 up four whole rows per lane spilled:
+// n = 32 12.04 against 6.74 ms.)
 template <int N>
-__host__ __device__ constexpr int rows_lanes() { return N == 18 ? 8 : 16; }
+__host__ __device__ constexpr int rows_lanes() { return (N >= 17 && N <= 20) ? 8 : 16; }
 
 template <int N, int LN = rows_lanes<N>()>
 struct RowsGeom {
