@@ -34,11 +34,13 @@ constexpr int kRowsMin = 16;        // smallest n of this kernel (partial pivoti
 // or 8 (four matrices per warp, up to four rows per lane).  Measured on GB300
 // at 1,000,000 matrices, same bits, with each step's search inside the
 // previous step: 8 lanes at n = 17 1.69 against 2.09 ms, 18 1.82 against
-// 2.30, 19 2.02 against 2.70, 20 1.95 against 2.35.  (Before that change 8
+// 2.30, 19 2.02 against 2.70, 20 1.95 against 2.35, 21 2.75 against 3.20,
+// 22 2.93 against 3.38, 23 3.27 against 3.67, 24 3.10 against 3.79; at
+// n = 25 (four rows per lane) 4.47 against 4.24.  (Before that change 8
 // lanes won only at n = 18; from n = 25 up four whole rows per lane spilled:
 // n = 32 12.04 against 6.74 ms.)
 template <int N>
-__host__ __device__ constexpr int rows_lanes() { return (N >= 17 && N <= 20) ? 8 : 16; }
+__host__ __device__ constexpr int rows_lanes() { return (N >= 17 && N <= 24) ? 8 : 16; }
 
 template <int N, int LN = rows_lanes<N>()>
 struct RowsGeom {

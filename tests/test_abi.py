@@ -149,10 +149,10 @@ def test_query_launch_reports_the_form_each_call_runs(lib):
     assert q(20, "reference", 1000, 300)[3] == 256
     assert q(20, "reference", 1000, 0)[3] == lib_tuned(lib, 20, 1)
     # partial pivoting: whole rows per lane at n = 16..32, eight lanes per
-    # matrix (four matrices per warp) at n = 17..20, sixteen elsewhere
-    for n in (16, 21, 24, 28, 29, 30, 31, 32):
+    # matrix (four matrices per warp) at n = 17..24, sixteen elsewhere
+    for n in (16, 25, 28, 29, 30, 31, 32):
         assert q(n, "partial", 10**6, 64) == ("rows", 16, 2, 128, False), n
-    for n in (17, 18, 19, 20):
+    for n in (17, 18, 20, 21, 24):
         assert q(n, "partial", 10**6, 64) == ("rows", 8, 4, 128, False), n
     # n = 32 without partial pivoting: eight lanes per matrix, four matrices per warp
     assert q(32, "reference", 10**6, 128) == ("lanes", 8, 4, 128, True)
