@@ -238,3 +238,19 @@ def test_device_error_query_reports_cuda_failure_without_gpu(lib):
     assert lib.mi_device_error(ctypes.byref(v), 1) == _lib.MI_ERR_CUDA
     assert v.value == -7                                   # untouched on failure
     assert b"device error word" in lib.mi_last_cuda_error()
+
+
+def test_persistent_walk_units_are_relocatable():
+    """The single persistent descriptor launch calls walks defined in other
+    units: every unit that defines or calls them must be compiled as
+    relocatable device code and device-linked, or the library link fails."""
+    import glob
+    import os
+
+    from matrixinversion_gb300 import build as B
+
+    units = {os.path.basename(p) for p in glob.glob(os.path.join(B.CSRC, "*.cu"))}
+    callers = {u for u in units if "MI_PWALK_" in open(os.path.join(B.CSRC, u)).read()}
+    assert callers == {"mi_descr_persist.cu", "mi_pwalk_none.cu", "mi_pwalk_reference.cu",
+                       "mi_pwalk_reference_serial.cu", "mi_pwalk_partial.cu"}
+    assert B.RDC_UNITS == callers
